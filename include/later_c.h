@@ -1,0 +1,106 @@
+/*
+ * later_c.h — C ABI of the GB300 (sm_103a) recursive QR / Cholesky library.
+ *
+ * Every entry point takes plain device pointers, sizes and leading dimensions
+ * (column-major, element (i,j) at A[i + j*lda]), runs asynchronously on the
+ * given CUDA stream and returns a later_status_t for argument / launch errors.
+ * Failures detected on the device (a bounded wait that gave up, an FP16 range
+ * overflow, a non-positive Cholesky pivot) are collected in a per-device
+ * status word; later_c_device_status() synchronises and returns it.
+ *
+ * Buffers follow the reference interface (include/LATER.h of LATER): the
+ * caller owns A, R, W and two workspaces — `work` (float) and `hwork` (16-bit)
+ * — whose minimum sizes the *_bufsize queries return. Nothing on these paths
+ * allocates device memory.
+ */
+#ifndef LATER_C_H
+#define LATER_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* later_stream_t; /* same type as cudaStream_t */
+
+typedef enum {
+  LATER_OK = 0,
+  LATER_ERR_INVALID_ARG = 1, /* bad size / leading dimension / flag */
+  LATER_ERR_WORKSPACE = 2,   /* work or hwork smaller than the *_bufsize query */
+  LATER_ERR_CUDA = 3,        /* a CUDA runtime call or launch failed */
+  LATER_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+  LATER_ERR_NOT_SUPPORTED = 5,
+  LATER_ERR_RANGE = 6,       /* a value exceeded the FP16 operand range: use BF16 */
+  LATER_ERR_NUMERIC = 7      /* non-positive pivot (matrix not SPD) */
+} later_status_t;
+
+typedef enum {
+  LATER_PREC_FP16 = 0,  /* FP16 tensor-core products, FP32 accumulation (reference behaviour) */
+  LATER_PREC_BF16 = 1,  /* BF16 products, FP32 accumulation (range-safe) */
+  LATER_PREC_SPLIT3 = 2 /* hi+lo FP16 split, three products per GEMM: ~FP32 accuracy */
+} later_precision_t;
+
+typedef struct {
+  int precision;            /* later_precision_t for every tensor-core GEMM */
+  int cgs2;                 /* 1: second Gram-Schmidt pass in every panel (CGS2) */
+  int leaf;                 /* rgsqrf leaf width: 32, 64 or 128 (0 = 128, the reference's NMIN) */
+  int reserved;
+  long long timeout_cycles; /* bound on every device wait in SM cycles (0 = about one second) */
+} later_options_t;
+
+/* Fills the defaults: FP16, no CGS2, leaf 128, default timeout. */
+void later_c_default_options(later_options_t* opt);
+
+const char* later_c_status_string(later_status_t s);
+
+/* Synchronises `stream`, then returns and clears the device status word. */
+later_status_t later_c_device_status(later_stream_t stream);
+
+/* ------------------------------------------------------------------ QR */
+
+/* Minimum `work` (floats) and `hwork` (16-bit elements) for later_c_rgsqrf. */
+later_status_t later_c_rgsqrf_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork,
+                                      int64_t* lhwork);
+
+/*
+ * Recursive Gram-Schmidt QR, A = Q R.
+ * Replaces LATER include/LATER.h:39 later_rgsqrf (QR/later_rgsqrf.cu:62-79).
+ * A (m x n, lda >= m) is overwritten by Q; R (n x n, ldr >= n) receives the
+ * upper-triangular factor with a positive diagonal and zeros below it.
+ * Requires m >= n >= 1 and n a multiple of 32.
+ */
+later_status_t later_c_rgsqrf(later_stream_t stream, int m, int n, float* A, int lda, float* R, int ldr,
+                              float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                              const later_options_t* opt);
+
+/* --------------------------------------------------------- building blocks */
+
+/*
+ * Tensor-core GEMM on 16-bit operands with FP32 accumulation:
+ *   D = alpha * op(A) * op(B) + beta * C      (op(X) = X or X^T by 'N' / 'T')
+ * A, B hold FP16 (precision FP16) or BF16 (precision BF16) elements; lda, ldb
+ * must be multiples of 8 and the pointers 16-byte aligned. C and D are FP32
+ * and may alias. `work` (floats) holds split-K partial sums; lwork = 0 turns
+ * split-K off. This is the kernel under every trailing update of
+ * QR/later_rgsqrf.cu:45-56 (cublasGemmEx sites in the reference).
+ */
+later_status_t later_c_gemm16(later_stream_t stream, char transa, char transb, int m, int n, int k,
+                              float alpha, const void* A, int lda, const void* B, int ldb, float beta,
+                              const float* C, int ldc, float* D, int ldd, int precision, float* work,
+                              int64_t lwork);
+
+/*
+ * FP32 -> 16-bit conversion of an m x n column-major block (the role of
+ * util/util.cu:24-32 s2h). precision FP16 / BF16 writes `hi`; SPLIT3 writes
+ * hi = fp16(x) and lo = fp16((x - hi) * 2048).
+ */
+later_status_t later_c_convert(later_stream_t stream, int m, int n, const float* A, int lda, void* hi,
+                               void* lo, int ldh, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LATER_C_H */

@@ -1,0 +1,177 @@
+"""GB300 (sm_103a) recursive QR / Cholesky — Python host side.
+
+The compute path is the shared library `later_gb300/_lib/liblater_gb300.so`
+(hand-written CUDA for sm_103a behind the C ABI of `include/later_c.h`). This
+module binds that ABI with ctypes and mirrors the reference's entry points
+(`later_rgsqrf`, ... of LATER's include/LATER.h) for torch CUDA tensors in
+column-major layout: a (m, n) tensor with stride (1, lda).
+
+There is no CPU or PyTorch fallback: if the library is missing, every entry
+point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+from . import build as _build
+
+__all__ = [
+    "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
+    "later_rgsqrf", "rgsqrf_bufsize", "gemm16", "convert16", "device_status",
+]
+
+PREC = {"fp16": 0, "bf16": 1, "split3": 2}
+STATUS = {0: "ok", 1: "invalid argument", 2: "workspace too small", 3: "CUDA runtime error",
+          4: "device wait timed out", 5: "not supported", 6: "value outside the FP16 operand range",
+          7: "non-positive pivot"}
+
+
+class LaterError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__(f"{where}: {STATUS.get(status, status)} (status {status})")
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("cgs2", ctypes.c_int), ("leaf", ctypes.c_int),
+                ("reserved", ctypes.c_int), ("timeout_cycles", ctypes.c_longlong)]
+
+    @classmethod
+    def make(cls, precision="fp16", cgs2=False, leaf=128, timeout_cycles=0) -> "Options":
+        p = PREC[precision] if isinstance(precision, str) else int(precision)
+        return cls(p, int(bool(cgs2)), int(leaf), 0, int(timeout_cycles))
+
+
+_lib = None
+_vp, _i, _i64, _f = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
+_SIGS = {
+    "later_c_default_options": (None, [ctypes.POINTER(Options)]),
+    "later_c_status_string": (ctypes.c_char_p, [_i]),
+    "later_c_device_status": (_i, [_vp]),
+    "later_c_rgsqrf_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "later_c_rgsqrf": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
+    "later_c_gemm16": (_i, [_vp, ctypes.c_char, ctypes.c_char, _i, _i, _i, _f, _vp, _i, _vp, _i, _f, _vp, _i,
+                            _vp, _i, _i, _vp, _i64]),
+    "later_c_convert": (_i, [_vp, _i, _i, _vp, _i, _vp, _vp, _i, _i]),
+}
+
+
+def lib_path() -> Path:
+    return _build.LIB
+
+
+def lib() -> ctypes.CDLL:
+    """Loads the shared library (building it first if the sources are newer)."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if os.environ.get("LATER_GB300_NO_BUILD") != "1":
+            path = _build.build()
+        if not path.exists():
+            raise RuntimeError(f"later_gb300: shared library {path} is missing; run later_gb300.build.build()")
+        l = ctypes.CDLL(str(path))
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+# ------------------------------------------------------------------ helpers
+def colmajor(t):
+    """Column-major copy of a 2-D tensor (stride (1, rows))."""
+    return t.t().contiguous().t()
+
+
+def empty_colmajor(m, n, dtype=None, device="cuda", ld=None):
+    import torch
+    ld = m if ld is None else ld
+    buf = torch.empty((n, ld), dtype=dtype or torch.float32, device=device)
+    return buf.t()[:m, :]
+
+
+def _ld(t, name) -> int:
+    if t.dim() != 2 or t.stride(0) != 1:
+        raise ValueError(f"{name} must be a column-major 2-D tensor (stride(0) == 1)")
+    return max(t.stride(1), t.shape[0], 1)
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _check(status: int, where: str):
+    if status != 0:
+        raise LaterError(status, where)
+
+
+def device_status(stream=None) -> int:
+    """Synchronises the stream and returns (and clears) the device status word."""
+    return lib().later_c_device_status(_stream(stream))
+
+
+def rgsqrf_bufsize(m, n, precision="fp16", cgs2=False, leaf=128):
+    o = Options.make(precision, cgs2, leaf)
+    lw, lh = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().later_c_rgsqrf_bufsize(m, n, ctypes.byref(o), ctypes.byref(lw), ctypes.byref(lh)), "rgsqrf_bufsize")
+    return lw.value, lh.value
+
+
+def later_rgsqrf(A, R=None, work=None, hwork=None, *, precision="fp16", cgs2=False, leaf=128, timeout_cycles=0,
+                 stream=None):
+    """Recursive Gram-Schmidt QR in place: A (m x n, column-major FP32 CUDA) becomes Q; returns R.
+
+    Mirrors LATER's `later_rgsqrf(ctxt, m, n, A, lda, R, ldr, work, lwork, hwork, lhwork)`
+    (include/LATER.h:39). Workspaces are allocated here when not given.
+    """
+    import torch
+    m, n = A.shape
+    lda = _ld(A, "A")
+    if R is None:
+        R = empty_colmajor(n, n, device=A.device)
+    ldr = _ld(R, "R")
+    lw, lh = rgsqrf_bufsize(m, n, precision, cgs2, leaf)
+    if work is None:
+        work = torch.empty(lw, dtype=torch.float32, device=A.device)
+    if hwork is None:
+        hwork = torch.empty(lh, dtype=torch.float16, device=A.device)
+    o = Options.make(precision, cgs2, leaf, timeout_cycles)
+    _check(lib().later_c_rgsqrf(_stream(stream), m, n, A.data_ptr(), lda, R.data_ptr(), ldr, work.data_ptr(),
+                                work.numel(), hwork.data_ptr(), hwork.numel(), ctypes.byref(o)), "later_rgsqrf")
+    return R
+
+
+def gemm16(transa, transb, A, B, alpha=1.0, beta=0.0, C=None, D=None, precision="fp16", work=None, stream=None):
+    """D = alpha op(A) op(B) + beta C on the tensor cores; A, B 16-bit column-major, C/D FP32."""
+    import torch
+    ta, tb = transa.upper(), transb.upper()
+    m = A.shape[0] if ta == "N" else A.shape[1]
+    k = A.shape[1] if ta == "N" else A.shape[0]
+    n = B.shape[1] if tb == "N" else B.shape[0]
+    if D is None:
+        D = empty_colmajor(m, n, device=A.device)
+    lda, ldb, ldd = _ld(A, "A"), _ld(B, "B"), _ld(D, "D")
+    ldc = _ld(C, "C") if C is not None else m
+    wp, wn = (work.data_ptr(), work.numel()) if work is not None else (None, 0)
+    _check(lib().later_c_gemm16(_stream(stream), ta.encode(), tb.encode(), m, n, k, alpha, A.data_ptr(), lda,
+                                B.data_ptr(), ldb, beta, C.data_ptr() if C is not None else None, ldc,
+                                D.data_ptr(), ldd, PREC[precision], wp, wn), "gemm16")
+    return D
+
+
+def convert16(A, precision="fp16", stream=None):
+    """FP32 -> 16-bit copy (SPLIT3: returns (hi, lo) with lo = fp16((x - hi) * 2048))."""
+    import torch
+    m, n = A.shape
+    dt = torch.bfloat16 if precision == "bf16" else torch.float16
+    ldh = (m + 7) // 8 * 8
+    hi = empty_colmajor(m, n, dtype=dt, device=A.device, ld=ldh)
+    lo = empty_colmajor(m, n, dtype=dt, device=A.device, ld=ldh) if precision == "split3" else None
+    _check(lib().later_c_convert(_stream(stream), m, n, A.data_ptr(), _ld(A, "A"), hi.data_ptr(),
+                                 lo.data_ptr() if lo is not None else None, ldh, PREC[precision]), "convert16")
+    return (hi, lo) if precision == "split3" else hi

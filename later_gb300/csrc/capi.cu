@@ -1,0 +1,108 @@
+// extern "C" entry points (include/later_c.h). Argument checking and status
+// mapping live here; the work is in the drivers.
+#include <cuda_runtime.h>
+
+#include "../../include/later_c.h"
+#include "qr.cuh"
+#include "runtime.cuh"
+
+using namespace later;
+
+extern "C" {
+
+void later_c_default_options(later_options_t* opt) {
+  if (!opt) return;
+  opt->precision = LATER_PREC_FP16;
+  opt->cgs2 = 0;
+  opt->leaf = 128;
+  opt->reserved = 0;
+  opt->timeout_cycles = 0;
+}
+
+const char* later_c_status_string(later_status_t s) {
+  switch (s) {
+    case LATER_OK: return "ok";
+    case LATER_ERR_INVALID_ARG: return "invalid argument";
+    case LATER_ERR_WORKSPACE: return "workspace too small";
+    case LATER_ERR_CUDA: return "CUDA runtime error";
+    case LATER_ERR_TIMEOUT: return "device wait timed out";
+    case LATER_ERR_NOT_SUPPORTED: return "not supported";
+    case LATER_ERR_RANGE: return "value outside the FP16 operand range";
+    case LATER_ERR_NUMERIC: return "non-positive pivot";
+  }
+  return "unknown status";
+}
+
+later_status_t later_c_device_status(later_stream_t stream) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return LATER_ERR_CUDA;
+  int* p = device_status_ptr();
+  if (!p) return LATER_ERR_CUDA;
+  int v = 0;
+  if (cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return LATER_ERR_CUDA;
+  if (v != 0 && cudaMemset(p, 0, sizeof(int)) != cudaSuccess) return LATER_ERR_CUDA;
+  if (v & DEV_TIMEOUT) return LATER_ERR_TIMEOUT;
+  if (v & DEV_NUMERIC) return LATER_ERR_NUMERIC;
+  if (v & DEV_RANGE) return LATER_ERR_RANGE;
+  return LATER_OK;
+}
+
+later_status_t later_c_rgsqrf_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork, int64_t* lhwork) {
+  if (m < 1 || n < 1 || m < n) return LATER_ERR_INVALID_ARG;
+  const QrNeed q = rgsqrf_need(m, n, options_from(opt));
+  if (lwork) *lwork = q.rec_work;
+  if (lhwork) *lhwork = q.hwork;
+  return LATER_OK;
+}
+
+later_status_t later_c_rgsqrf(later_stream_t stream, int m, int n, float* A, int lda, float* R, int ldr,
+                              float* work, int64_t lwork, void* hwork, int64_t lhwork, const later_options_t* opt) {
+  return rgsqrf(reinterpret_cast<cudaStream_t>(stream), m, n, A, lda, R, ldr, work, lwork, hwork, lhwork,
+                options_from(opt));
+}
+
+later_status_t later_c_gemm16(later_stream_t stream, char transa, char transb, int m, int n, int k, float alpha,
+                              const void* A, int lda, const void* B, int ldb, float beta, const float* C, int ldc,
+                              float* D, int ldd, int precision, float* work, int64_t lwork) {
+  auto ok_t = [](char t) { return t == 'N' || t == 'n' || t == 'T' || t == 't'; };
+  if (!ok_t(transa) || !ok_t(transb) || m < 0 || n < 0 || k < 1 || !A || !B || !D) return LATER_ERR_INVALID_ARG;
+  if (precision != LATER_PREC_FP16 && precision != LATER_PREC_BF16) return LATER_ERR_INVALID_ARG;
+  const bool an = (transa == 'N' || transa == 'n');
+  const bool bn = (transb == 'N' || transb == 'n');
+  if (lda < (an ? m : k) || ldb < (bn ? k : n) || ldd < m || (beta != 0.f && (!C || ldc < m)))
+    return LATER_ERR_INVALID_ARG;
+  GemmCall g;
+  g.ta = transa;
+  g.tb = transb;
+  g.M = m;
+  g.N = n;
+  g.K = k;
+  g.A = Op16{A, nullptr, lda};
+  g.B = Op16{B, nullptr, ldb};
+  g.alpha = alpha;
+  g.beta = beta;
+  g.out.C = C;
+  g.out.ldc = ldc;
+  g.out.D = D;
+  g.out.ldd = ldd;
+  g.prec = precision;
+  Scratch s;
+  if (work && lwork > 4096 * 2) {
+    s.counters = reinterpret_cast<int*>(work);
+    s.n_counters = 4096;
+    s.partial = work + 4096;
+    s.partial_floats = lwork - 4096;
+    if (cudaMemsetAsync(s.counters, 0, 4096 * sizeof(int), reinterpret_cast<cudaStream_t>(stream)) != cudaSuccess)
+      return LATER_ERR_CUDA;
+  }
+  return tc_gemm(g, s, reinterpret_cast<cudaStream_t>(stream), 0);
+}
+
+later_status_t later_c_convert(later_stream_t stream, int m, int n, const float* A, int lda, void* hi, void* lo,
+                               int ldh, int precision) {
+  if (m < 0 || n < 0 || !A || !hi || lda < m || ldh < m) return LATER_ERR_INVALID_ARG;
+  if (precision < LATER_PREC_FP16 || precision > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;
+  return convert16(reinterpret_cast<cudaStream_t>(stream), m, n, A, lda, hi, lo, ldh, precision);
+}
+
+}  // extern "C"

@@ -1,0 +1,447 @@
+// Tensor-core GEMM for sm_103a: TMA-fed, tcgen05.mma with the accumulator in
+// TMEM, FP16 / BF16 operands and FP32 accumulation.
+//
+//   D = alpha * op(A) * op(B) + beta * C,   column-major, op = N or T.
+//
+// This is the kernel behind every trailing update of the recursion drivers.
+// In the reference those are cublasGemmEx calls on FP16 copies produced by
+// separate s2h passes (QR/later_rgsqrf.cu:43-56, QR/later_rhouqr.cu:111-134,
+// BLAS/later_rsyrk.cu:38-65, BLAS/later_rtrsm.cu:101-112,150-160,
+// BLAS/later_rtrmm.cu:40-51). Here the epilogue writes the FP32 result and,
+// when asked, its 16-bit copy in the same pass, so the next GEMM of the
+// recursion reads its operand without a conversion pass.
+//
+// Structure (one CTA = one 128 x BN output tile, or one K-slice of it):
+//   warp 0 / lane 0 : TMA producer, STAGES-deep ring of 64-wide K blocks
+//   warp 1 / lane 0 : MMA issuer (tcgen05.mma, M=128, N=BN, K=16 steps);
+//                     warp 1 also owns the TMEM allocation
+//   warps 0-3       : epilogue, one TMEM lane quarter (32 rows) per warp
+// Split-K: CTAs of one tile write FP32 partial tiles; the last one to finish
+// (atomic ticket) sums them in split order, so results are deterministic.
+// SPLIT3: A = Ah + Al/2048, B = Bh + Bl/2048 (FP16); three products go to two
+// TMEM accumulators, D = acc0 + acc1/2048.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "ptx.cuh"
+#include "runtime.cuh"
+
+namespace later {
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int BK = 64;
+constexpr float kLoScale = 2048.f;       // SPLIT3 lo operands are stored scaled by 2^11
+constexpr float kLoScaleInv = 1.f / 2048.f;
+
+struct GemmArgs {
+  int M, N, K;
+  int kb_total, kb_per_split, splits;
+  int tiles_m;
+  float alpha, beta;
+  const float* C;
+  int64_t ldc;
+  float* D;
+  int64_t ldd;
+  void* Dh;
+  void* Dl;
+  int64_t ldh;
+  int out_mode;  // 0 fp16, 1 bf16, 2 split3 (hi/lo fp16)
+  int lower, diag;
+  int shadow_acc;
+  int ab_bf16;
+  float* partial;
+  int* counters;
+  int* status;
+  long long budget;
+};
+
+__device__ __forceinline__ void store16(void* base, int64_t idx, float v, int bf16) {
+  if (bf16)
+    reinterpret_cast<__nv_bfloat16*>(base)[idx] = __float2bfloat16_rn(v);
+  else
+    reinterpret_cast<__half*>(base)[idx] = __float2half_rn(v);
+}
+
+template <int BN, bool A_MN, bool B_MN, bool SPLIT, int STAGES>
+struct Cfg {
+  static constexpr int A_BYTES = BM * BK * 2;  // 16 KB
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int NOPS = SPLIT ? 2 : 1;
+  static constexpr int STAGE_BYTES = NOPS * (A_BYTES + B_BYTES);
+  static constexpr int TMEM_COLS = SPLIT ? 2 * BN : BN;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+template <int BN, bool A_MN, bool B_MN, bool SPLIT, int STAGES>
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const __grid_constant__ CUtensorMap tmAl, const __grid_constant__ CUtensorMap tmBl,
+                   const GemmArgs p) {
+  using C_ = Cfg<BN, A_MN, B_MN, SPLIT, STAGES>;
+  static_assert(C_::TMEM_COLS >= 32 && C_::TMEM_COLS <= 512, "tmem");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * C_::STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* done = empty + STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* last_flag = abort_flag + 1;
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int tile_m = blockIdx.x % p.tiles_m;
+  const int tile_n = blockIdx.x / p.tiles_m;
+  const int split = blockIdx.y;
+  const int m0 = tile_m * BM;
+  const int n0 = tile_n * BN;
+  const int kb0 = split * p.kb_per_split;
+  const int kb1 = min(kb0 + p.kb_per_split, p.kb_total);
+  const int nkb = kb1 - kb0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    *last_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, C_::TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ------------------------------------------------------- producer
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      if (SPLIT) {
+        tma_prefetch_desc(&tmAl);
+        tma_prefetch_desc(&tmBl);
+      }
+      int issued = 0;
+      for (int i = 0; i < nkb; ++i) {
+        const int s = i % STAGES;
+        const uint32_t ph = (i / STAGES) & 1;
+        if (i >= STAGES && !mbar_wait(&empty[s], ph ^ 1, p.budget)) {
+          *abort_flag = 1;
+          break;
+        }
+        if (*abort_flag) break;
+        uint8_t* sa = smem + s * C_::STAGE_BYTES;
+        uint8_t* sb = sa + C_::NOPS * C_::A_BYTES;
+        const int k0 = (kb0 + i) * BK;
+        mbar_arrive_expect_tx(&full[s], C_::STAGE_BYTES);
+#pragma unroll
+        for (int op = 0; op < C_::NOPS; ++op) {
+          const CUtensorMap* ma = op ? &tmAl : &tmA;
+          const CUtensorMap* mb = op ? &tmBl : &tmB;
+          uint8_t* da = sa + op * C_::A_BYTES;
+          uint8_t* db = sb + op * C_::B_BYTES;
+          if (A_MN) {
+            tma_load_2d(da, ma, &full[s], m0, k0);
+            tma_load_2d(da + BK * 128, ma, &full[s], m0 + 64, k0);
+          } else {
+            tma_load_2d(da, ma, &full[s], k0, m0);
+          }
+          if (B_MN) {
+#pragma unroll
+            for (int c = 0; c < BN / 64; ++c) tma_load_2d(db + c * BK * 128, mb, &full[s], n0 + 64 * c, k0);
+          } else {
+            tma_load_2d(db, mb, &full[s], k0, n0);
+          }
+        }
+        ++issued;
+      }
+      // Drain: every issued load must land before the CTA may exit.
+      for (int j = (issued > STAGES ? issued - STAGES : 0); j < issued; ++j)
+        mbar_wait(&full[j % STAGES], (j / STAGES) & 1, kDrainBudgetCycles);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ------------------------------------------------------- MMA issuer
+      const uint32_t idesc = idesc_f16(BM, BN, p.ab_bf16, A_MN ? 1 : 0, B_MN ? 1 : 0);
+      for (int i = 0; i < nkb; ++i) {
+        const int s = i % STAGES;
+        const uint32_t ph = (i / STAGES) & 1;
+        if (!mbar_wait(&full[s], ph, p.budget)) {
+          *abort_flag = 1;
+          break;
+        }
+        if (*abort_flag) break;
+        tc_fence_after();
+        const uint32_t sa = smem_u32(smem + s * C_::STAGE_BYTES);
+        const uint32_t sb = sa + C_::NOPS * C_::A_BYTES;
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k) {
+          // A: K-major -> advance 32 B within the swizzled row; MN-major -> 16 K-rows.
+          const uint32_t a_off = A_MN ? k * 16 * 128 : k * 32;
+          const uint32_t b_off = B_MN ? k * 16 * 128 : k * 32;
+          const uint64_t ad = smem_desc_sw128(sa + a_off, A_MN ? BK * 128 : 16, 1024);
+          const uint64_t bd = smem_desc_sw128(sb + b_off, B_MN ? BK * 128 : 16, 1024);
+          const uint32_t acc = (i > 0 || k > 0) ? 1u : 0u;
+          tc_mma_f16(tmem, ad, bd, idesc, acc);
+          if (SPLIT) {
+            const uint64_t adl = smem_desc_sw128(sa + C_::A_BYTES + a_off, A_MN ? BK * 128 : 16, 1024);
+            const uint64_t bdl = smem_desc_sw128(sb + C_::B_BYTES + b_off, B_MN ? BK * 128 : 16, 1024);
+            tc_mma_f16(tmem + BN, ad, bdl, idesc, acc);
+            tc_mma_f16(tmem + BN, adl, bd, idesc, 1u);
+          }
+        }
+        tc_commit(&empty[s]);
+      }
+      tc_commit(done);  // arrives once every MMA above has completed
+    }
+  }
+  __syncwarp();
+
+  // --------------------------------------------------------------- epilogue
+  const bool drained = mbar_wait(done, 0, kDrainBudgetCycles);
+  tc_fence_after();
+  const bool ok = drained && (*abort_flag == 0) && nkb > 0;
+  if (!ok && threadIdx.x == 0) report(p.status, DEV_TIMEOUT);
+
+  const int r = warp * 32 + lane;  // tile row == TMEM lane
+  const int row = m0 + r;
+  const uint32_t t_row = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+  const int out16 = (p.Dh != nullptr);
+
+  auto finish = [&](int col, float acc) {
+    if (row >= p.M || col >= p.N) return;
+    if (p.lower && row < col + p.diag) return;
+    const float prod = p.alpha * acc;
+    float v = prod;
+    if (p.beta != 0.f) v += p.beta * p.C[row + static_cast<int64_t>(col) * p.ldc];
+    p.D[row + static_cast<int64_t>(col) * p.ldd] = v;
+    if (out16) {
+      if (p.shadow_acc) v = prod;
+      const int64_t hidx = row + static_cast<int64_t>(col) * p.ldh;
+      if (p.out_mode == 1) {
+        store16(p.Dh, hidx, v, 1);
+      } else {
+        if (fabsf(v) > 65504.f) report(p.status, DEV_RANGE);
+        const __half h = __float2half_rn(v);
+        reinterpret_cast<__half*>(p.Dh)[hidx] = h;
+        if (p.out_mode == 2)
+          reinterpret_cast<__half*>(p.Dl)[hidx] = __float2half_rn((v - __half2float(h)) * kLoScale);
+      }
+    }
+  };
+
+  if (p.splits == 1) {
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      tmem_ld_32x32b_x32(t_row + c0, v);
+      if (SPLIT) {
+        float w[32];
+        tmem_ld_32x32b_x32(t_row + BN + c0, w);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] += w[j] * kLoScaleInv;
+      }
+      if (ok) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) finish(n0 + c0 + j, v[j]);
+      }
+    }
+  } else {
+    const int tile = blockIdx.x;
+    float* mine = p.partial + (static_cast<int64_t>(tile) * p.splits + split) * (BM * BN);
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      float v[32];
+      tmem_ld_32x32b_x32(t_row + c0, v);
+      if (SPLIT) {
+        float w[32];
+        tmem_ld_32x32b_x32(t_row + BN + c0, w);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] += w[j] * kLoScaleInv;
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j) __stcg(&mine[(c0 + j) * BM + r], ok ? v[j] : 0.f);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int prev = atomicAdd(&p.counters[tile], 1);
+      *last_flag = (prev == p.splits - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (*last_flag) {
+      __threadfence();
+      const float* base = p.partial + static_cast<int64_t>(tile) * p.splits * (BM * BN);
+#pragma unroll 1
+      for (int c = 0; c < BN; ++c) {
+        float acc = 0.f;
+#pragma unroll 1
+        for (int s = 0; s < p.splits; ++s) acc += __ldcg(&base[static_cast<int64_t>(s) * (BM * BN) + c * BM + r]);
+        finish(n0 + c, acc);
+      }
+      if (threadIdx.x == 0) p.counters[tile] = 0;
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) tmem_dealloc(tmem, C_::TMEM_COLS);
+}
+
+// ------------------------------------------------------------------- host
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  });
+  return fn;
+}
+
+template <int BN, bool A_MN, bool B_MN, bool SPLIT, int STAGES>
+later_status_t launch_cfg(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& al,
+                          const CUtensorMap& bl, const GemmArgs& args, dim3 grid, cudaStream_t st) {
+  using C_ = Cfg<BN, A_MN, B_MN, SPLIT, STAGES>;
+  auto kern = tc_gemm_kernel<BN, A_MN, B_MN, SPLIT, STAGES>;
+  static bool attr_done[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr_done[dev]) {
+    LATER_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C_::SMEM));
+    attr_done[dev] = true;
+  }
+  kern<<<grid, 128, C_::SMEM, st>>>(a, b, al, bl, args);
+  return cuda_status(cudaGetLastError());
+}
+
+template <int BN, bool SPLIT, int STAGES>
+later_status_t launch_bn(bool a_mn, bool b_mn, const CUtensorMap& a, const CUtensorMap& b,
+                         const CUtensorMap& al, const CUtensorMap& bl, const GemmArgs& args, dim3 grid,
+                         cudaStream_t st) {
+  if (!a_mn && !b_mn) return launch_cfg<BN, false, false, SPLIT, STAGES>(a, b, al, bl, args, grid, st);
+  if (a_mn && !b_mn) return launch_cfg<BN, true, false, SPLIT, STAGES>(a, b, al, bl, args, grid, st);
+  if (a_mn && b_mn) return launch_cfg<BN, true, true, SPLIT, STAGES>(a, b, al, bl, args, grid, st);
+  return launch_cfg<BN, false, true, SPLIT, STAGES>(a, b, al, bl, args, grid, st);
+}
+
+}  // namespace
+
+bool make_map16(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint64_t ld,
+                uint32_t box_rows, uint32_t box_cols, bool bf16) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ld * 2) % 16 != 0) return false;
+  cuuint64_t dims[2] = {rows, cols};
+  cuuint64_t strides[1] = {ld * 2};
+  cuuint32_t box[2] = {box_rows, box_cols};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                  const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, long long budget) {
+  if (g.M <= 0 || g.N <= 0) return LATER_OK;
+  if (g.K <= 0) return LATER_ERR_INVALID_ARG;
+  const bool a_mn = (g.ta == 'N' || g.ta == 'n');
+  const bool b_mn = (g.tb == 'T' || g.tb == 't');
+  const bool split3 = (g.prec == LATER_PREC_SPLIT3);
+  const bool bf16 = (g.prec == LATER_PREC_BF16);
+  if (split3 && (!g.A.lo || !g.B.lo)) return LATER_ERR_INVALID_ARG;
+  if (g.out.Dh && g.out_prec == LATER_PREC_SPLIT3 && !g.out.Dl) return LATER_ERR_INVALID_ARG;
+
+  // Tile width: the widest of 256 / 128 / 64 that still gives the GPU enough tiles.
+  const int nsm = num_sms();
+  const int tiles_m = static_cast<int>((g.M + BM - 1) / BM);
+  int BN = 128;
+  if (!split3 && static_cast<int64_t>(tiles_m) * ((g.N + 255) / 256) >= nsm) BN = 256;
+  if (g.N <= 64) BN = 64;
+  const int tiles_n = (g.N + BN - 1) / BN;
+  const int tiles = tiles_m * tiles_n;
+  const int kb_total = (g.K + BK - 1) / BK;
+
+  // Split-K when the tile grid leaves SMs idle; at least 4 K blocks per split.
+  int splits = 1;
+  if (tiles < nsm && s.partial && s.counters && tiles <= s.n_counters) {
+    int want = (nsm + tiles - 1) / tiles;
+    int maxk = kb_total / 4;
+    splits = want < maxk ? want : maxk;
+    const int64_t per = static_cast<int64_t>(tiles) * BM * BN;
+    const int64_t fit = per > 0 ? s.partial_floats / per : 0;
+    if (splits > fit) splits = static_cast<int>(fit);
+    if (splits < 1) splits = 1;
+  }
+  int kb_per_split = (kb_total + splits - 1) / splits;
+  splits = (kb_total + kb_per_split - 1) / kb_per_split;
+
+  GemmArgs a{};
+  a.M = g.M;
+  a.N = g.N;
+  a.K = g.K;
+  a.kb_total = kb_total;
+  a.kb_per_split = kb_per_split;
+  a.splits = splits;
+  a.tiles_m = tiles_m;
+  a.alpha = g.alpha;
+  a.beta = g.beta;
+  a.C = g.out.C;
+  a.ldc = g.out.ldc;
+  a.D = g.out.D;
+  a.ldd = g.out.ldd;
+  a.Dh = g.out.Dh;
+  a.Dl = g.out.Dl;
+  a.ldh = g.out.ldh;
+  a.out_mode = g.out_prec == LATER_PREC_BF16 ? 1 : (g.out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
+  a.lower = g.out.lower;
+  a.diag = g.out.diag;
+  a.shadow_acc = g.out.shadow_acc;
+  a.ab_bf16 = bf16 ? 1 : 0;
+  a.partial = s.partial;
+  a.counters = s.counters;
+  a.status = device_status_ptr();
+  a.budget = budget > 0 ? budget : kDefaultBudgetCycles;
+
+  // Tensor maps over the stored (column-major) operands.
+  CUtensorMap ma{}, mb{}, mal{}, mbl{};
+  const uint64_t a_rows = a_mn ? g.M : g.K, a_cols = a_mn ? g.K : g.M;
+  const uint64_t b_rows = b_mn ? g.N : g.K, b_cols = b_mn ? g.K : g.N;
+  const uint32_t a_box_c = a_mn ? BK : BM;
+  const uint32_t b_box_c = b_mn ? BK : BN;
+  if (!make_map16(&ma, g.A.hi, a_rows, a_cols, g.A.ld, 64, a_box_c, bf16)) return LATER_ERR_INVALID_ARG;
+  if (!make_map16(&mb, g.B.hi, b_rows, b_cols, g.B.ld, 64, b_box_c, bf16)) return LATER_ERR_INVALID_ARG;
+  if (split3) {
+    if (!make_map16(&mal, g.A.lo, a_rows, a_cols, g.A.ld, 64, a_box_c, false)) return LATER_ERR_INVALID_ARG;
+    if (!make_map16(&mbl, g.B.lo, b_rows, b_cols, g.B.ld, 64, b_box_c, false)) return LATER_ERR_INVALID_ARG;
+  } else {
+    mal = ma;
+    mbl = mb;
+  }
+
+  dim3 grid(tiles, splits);
+  if (split3) {
+    if (BN == 64) return launch_bn<64, true, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+    return launch_bn<128, true, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+  }
+  if (BN == 64) return launch_bn<64, false, 6>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+  if (BN == 128) return launch_bn<128, false, 4>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+  return launch_bn<256, false, 4>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+}
+
+}  // namespace later

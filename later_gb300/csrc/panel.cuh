@@ -1,0 +1,41 @@
+// Interfaces of the FP32 panel kernels (panel.cu) used by the drivers.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "runtime.cuh"
+
+namespace later {
+
+constexpr int kMaxTsqrLevels = 8;
+
+// One TSQR tree over an m x 32 panel. Level 0 is the panel itself; level
+// L >= 1 is the stack of the 32x32 R factors of level L-1 (32 rows per block).
+struct TsqrPlan {
+  int nlev;
+  float* lev[kMaxTsqrLevels];
+  int64_t ld[kMaxTsqrLevels];
+  int rows[kMaxTsqrLevels];
+  int nblk[kMaxTsqrLevels];
+  int cnt_off[kMaxTsqrLevels];
+  int* counters;
+  float* R;
+  int64_t ldr;
+};
+
+void tsqr_plan_sizes(int m, int* nlev, int rows[kMaxTsqrLevels], int nblk[kMaxTsqrLevels], int64_t* stack_floats,
+                     int* ncounters);
+
+// QR of the m x 32 panel A: Q overwrites A (FP32) and is also written to the
+// 16-bit copy (qh / ql, may be null); R (32x32, upper) goes to R.
+later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R, int64_t ldr, void* qh, void* ql,
+                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed);
+
+// R (+)= X^T Y for X (m x k1), Y (m x k2), k1, k2 <= 64, FP32.
+later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* Y,
+                       int64_t ldy, float* R, int64_t ldr, int accumulate, Arena& ws);
+
+// Y -= X S for X (m x k1), S (k1 x k2), k1, k2 <= 64, FP32.
+later_status_t simt_nn_sub(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* S,
+                           int64_t lds, float* Y, int64_t ldy);
+
+}  // namespace later

@@ -1,0 +1,235 @@
+// Recursive Gram-Schmidt QR driver (host side).
+//
+// Follows the recursion of the reference's later_rgsqrf (QR/later_rgsqrf.cu:25-79):
+//   [A1 | A2] = [Q1 | Q2] [R11 R12; 0 R22]
+//   qr(A1);  R12 = Q1^T A2;  A2 -= Q1 R12;  qr(A2)
+// with the leaf panel at n <= leaf (NMIN = 128 in the reference, :23).
+// Differences, all on the GB300 side of the boundary:
+//   * the 16-bit operand copy of A is kept up to date by the producers (panel
+//     apply and the A2 -= Q1 R12 epilogue), so there are no s2h passes;
+//   * R12 = Q1^T A2 splits K over idle SMs with a deterministic reduction;
+//   * the caller's lda is honoured (the reference passes m, :70);
+//   * R is written in full, zeros below the diagonal;
+//   * optional CGS2 (second projection pass) and SPLIT3 / BF16 precisions.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "panel.cuh"
+#include "qr.cuh"
+
+namespace later {
+
+Options options_from(const later_options_t* o) {
+  Options r;
+  if (!o) return r;
+  r.prec = o->precision;
+  r.cgs2 = o->cgs2 ? 1 : 0;
+  r.leaf = o->leaf > 0 ? o->leaf : 128;
+  r.budget = o->timeout_cycles > 0 ? o->timeout_cycles : kDefaultBudgetCycles;
+  return r;
+}
+
+namespace {
+
+constexpr int kCounters = 4096;  // ints: [0,2048) panels, [2048,4096) GEMM split-K
+
+struct Ctx {
+  cudaStream_t st;
+  Options o;
+  Arena* ws;        // float workspace (after the fixed regions)
+  int* counters;    // zeroed at the start of the call
+  char* sh_hi;      // 16-bit copy of A (column 0 of the full matrix)
+  char* sh_lo;      // SPLIT3 lo copy
+  int64_t ldh;
+  void* r12h;       // 16-bit copy of the current R12 (top-level size)
+  void* r12l;
+  int64_t ldr12;
+  float* s_tmp;     // CGS2 second-pass coefficients (top-level size)
+  int64_t lds;
+  int m;
+};
+
+inline char* col16(char* base, int64_t ld, int64_t j) { return base ? base + j * ld * 2 : nullptr; }
+
+Scratch gemm_scratch(Ctx& c) {
+  Scratch s;
+  s.counters = c.counters + 2048;
+  s.n_counters = 2048;
+  // Split-K partials use whatever the arena has left (never more than needed).
+  const int64_t avail = static_cast<int64_t>(c.ws->remaining() / sizeof(float)) - 64;
+  const int64_t cap = static_cast<int64_t>(num_sms()) * 128 * 256 * 2;
+  s.partial_floats = std::max<int64_t>(0, std::min(avail, cap));
+  s.partial = s.partial_floats > 0 ? reinterpret_cast<float*>(
+                                         (reinterpret_cast<uintptr_t>(c.ws->cursor()) + 255) & ~uintptr_t(255))
+                                   : nullptr;
+  if (s.partial_floats > 0) s.partial_floats -= 64;
+  return s;
+}
+
+later_status_t leaf_qr(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
+  if (w <= 32) {
+    return tsqr_panel(c.st, c.m, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
+                      c.o.prec, *c.ws, c.counters);
+  }
+  const int w1 = split_half(w), w2 = w - w1;
+  LATER_CHECK(leaf_qr(c, w1, A, lda, R, ldr, col));
+  float* A2 = A + w1 * lda;
+  float* R12 = R + w1 * ldr;
+  LATER_CHECK(simt_tn(c.st, c.m, w1, w2, A, lda, A2, lda, R12, ldr, 0, *c.ws));
+  LATER_CHECK(simt_nn_sub(c.st, c.m, w1, w2, A, lda, R12, ldr, A2, lda));
+  if (c.o.cgs2) {
+    LATER_CHECK(simt_tn(c.st, c.m, w1, w2, A, lda, A2, lda, c.s_tmp, c.lds, 0, *c.ws));
+    LATER_CHECK(simt_nn_sub(c.st, c.m, w1, w2, A, lda, c.s_tmp, c.lds, A2, lda));
+    LATER_CHECK(axpy2d(c.st, w1, w2, 1.f, c.s_tmp, c.lds, R12, ldr));
+  }
+  return leaf_qr(c, w2, A2, lda, R + w1 + w1 * ldr, ldr, col + w1);
+}
+
+later_status_t rec_qr(Ctx& c, int n, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
+  if (n <= c.o.leaf) return leaf_qr(c, n, A, lda, R, ldr, col);
+  const int n1 = split_half(n), n2 = n - n1;
+  LATER_CHECK(rec_qr(c, n1, A, lda, R, ldr, col));
+  float* A2 = A + n1 * lda;
+  float* R12 = R + n1 * ldr;
+  Op16 Q1{col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh};
+  Op16 A2h{col16(c.sh_hi, c.ldh, col + n1), col16(c.sh_lo, c.ldh, col + n1), c.ldh};
+  Op16 R12h{c.r12h, c.r12l, c.ldr12};
+  const int passes = c.o.cgs2 ? 2 : 1;
+  for (int pass = 0; pass < passes; ++pass) {
+    // R12 (+)= Q1^T A2, FP32 into R, 16-bit copy of this pass's product.
+    GemmCall tn;
+    tn.ta = 'T';
+    tn.tb = 'N';
+    tn.M = n1;
+    tn.N = n2;
+    tn.K = c.m;
+    tn.A = Q1;
+    tn.B = A2h;
+    tn.alpha = 1.f;
+    tn.beta = pass ? 1.f : 0.f;
+    tn.out.C = R12;
+    tn.out.ldc = ldr;
+    tn.out.D = R12;
+    tn.out.ldd = ldr;
+    tn.out.Dh = c.r12h;
+    tn.out.Dl = c.r12l;
+    tn.out.ldh = c.ldr12;
+    tn.out.shadow_acc = 1;
+    tn.prec = c.o.prec;
+    tn.out_prec = c.o.prec;
+    LATER_CHECK(tc_gemm(tn, gemm_scratch(c), c.st, c.o.budget));
+    // A2 -= Q1 R12 in FP32, refreshing A2's 16-bit copy.
+    GemmCall nn;
+    nn.ta = 'N';
+    nn.tb = 'N';
+    nn.M = c.m;
+    nn.N = n2;
+    nn.K = n1;
+    nn.A = Q1;
+    nn.B = R12h;
+    nn.alpha = -1.f;
+    nn.beta = 1.f;
+    nn.out.C = A2;
+    nn.out.ldc = lda;
+    nn.out.D = A2;
+    nn.out.ldd = lda;
+    nn.out.Dh = const_cast<void*>(A2h.hi);
+    nn.out.Dl = const_cast<void*>(A2h.lo);
+    nn.out.ldh = c.ldh;
+    nn.prec = c.o.prec;
+    nn.out_prec = c.o.prec;
+    LATER_CHECK(tc_gemm(nn, gemm_scratch(c), c.st, c.o.budget));
+  }
+  return rec_qr(c, n2, A2, lda, R + n1 + n1 * ldr, ldr, col + n1);
+}
+
+// Width of the first leaf the recursion reaches (its columns need no initial
+// 16-bit copy: the panel writes it).
+int first_leaf(int n, int leaf) {
+  while (n > leaf) n = split_half(n);
+  return n;
+}
+
+// Carves the fixed regions out of `work` (or sizes them when work is null).
+// Everything after them is shared, in stream order, by the panel tree stacks,
+// the leaf projection partials and the split-K partial tiles.
+struct Layout {
+  int* counters;
+  void* r12h;
+  void* r12l;
+  int64_t ldr12;
+  float* s_tmp;
+  int64_t lds;
+};
+
+bool carve(Arena& ws, int n, const Options& o, Layout* L) {
+  L->counters = ws.take<int>(kCounters);
+  const int n1 = n > o.leaf ? split_half(n) : 0;
+  const int n2 = n - n1;
+  const bool split3 = o.prec == LATER_PREC_SPLIT3;
+  L->ldr12 = round_up(std::max(n1, 8), 8);
+  L->r12h = n1 ? ws.take<uint16_t>(L->ldr12 * n2) : nullptr;
+  L->r12l = (n1 && split3) ? ws.take<uint16_t>(L->ldr12 * n2) : nullptr;
+  L->lds = 64;
+  L->s_tmp = o.cgs2 ? ws.take<float>(64 * 64) : nullptr;
+  return !ws.failed();
+}
+
+}  // namespace
+
+QrNeed rgsqrf_need(int m, int n, const Options& o) {
+  QrNeed q;
+  Arena a(nullptr, 0);
+  Layout L;
+  carve(a, n, o, &L);
+  const int64_t fixed = static_cast<int64_t>(a.peak() / sizeof(float)) + 64;
+  int nlev, rows[kMaxTsqrLevels], nblk[kMaxTsqrLevels], ncnt;
+  int64_t stack;
+  tsqr_plan_sizes(m, &nlev, rows, nblk, &stack, &ncnt);
+  stack += 64 * kMaxTsqrLevels;
+  const int64_t leaf_parts = ((m + 127) / 128) * 4096 + 128;
+  const int64_t splitk = static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 128;
+  q.min_work = fixed + std::max<int64_t>(stack, 4096 + 128);
+  q.rec_work = fixed + std::max(std::max(stack, leaf_parts), splitk);
+  const int64_t ldh = round_up(m, 8);
+  q.hwork = ldh * n * (o.prec == LATER_PREC_SPLIT3 ? 2 : 1) + 64;
+  return q;
+}
+
+later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, float* R, int64_t ldr, float* work,
+                      int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
+  if (m < 1 || n < 1 || m < n || n % 32 != 0 || lda < m || ldr < n || !A || !R) return LATER_ERR_INVALID_ARG;
+  if (o.leaf != 32 && o.leaf != 64 && o.leaf != 128) return LATER_ERR_INVALID_ARG;
+  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;
+  const QrNeed need = rgsqrf_need(m, n, o);
+  if (!work || !hwork || lwork < need.min_work || lhwork < need.hwork) return LATER_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(hwork) & 15) != 0) return LATER_ERR_INVALID_ARG;
+
+  Arena ws(work, static_cast<size_t>(lwork) * sizeof(float));
+  Layout L;
+  if (!carve(ws, n, o, &L)) return LATER_ERR_WORKSPACE;
+  Ctx c;
+  c.st = st;
+  c.o = o;
+  c.m = m;
+  c.ws = &ws;
+  c.counters = L.counters;
+  c.ldh = round_up(m, 8);
+  c.sh_hi = static_cast<char*>(hwork);
+  c.sh_lo = o.prec == LATER_PREC_SPLIT3 ? c.sh_hi + c.ldh * n * 2 : nullptr;
+  c.r12h = L.r12h;
+  c.r12l = L.r12l;
+  c.ldr12 = L.ldr12;
+  c.s_tmp = L.s_tmp;
+  c.lds = L.lds;
+
+  LATER_CHECK_CUDA(cudaMemsetAsync(L.counters, 0, kCounters * sizeof(int), st));
+  LATER_CHECK(fill_strict_lower(st, n, n, R, ldr, 0.f));
+  const int f = first_leaf(n, o.leaf);
+  LATER_CHECK(convert16(st, m, n - f, A + static_cast<int64_t>(f) * lda, lda, c.sh_hi + f * c.ldh * 2,
+                        c.sh_lo ? c.sh_lo + f * c.ldh * 2 : nullptr, c.ldh, o.prec));
+  return rec_qr(c, n, A, lda, R, ldr, 0);
+}
+
+}  // namespace later

@@ -1,0 +1,33 @@
+// Recursive QR drivers (host side): rgsqrf now, rhouqr / ormqr alongside.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "runtime.cuh"
+
+namespace later {
+
+struct Options {
+  int prec = LATER_PREC_FP16;
+  int cgs2 = 0;
+  int leaf = 128;
+  long long budget = kDefaultBudgetCycles;
+};
+
+Options options_from(const later_options_t* o);
+
+// Workspace need of later_c_rgsqrf: `min_*` is what the call refuses to run
+// below, `rec_*` what the *_bufsize query reports (adds room for split-K and
+// for fully parallel panel projections).
+struct QrNeed {
+  int64_t min_work = 0, rec_work = 0;  // floats
+  int64_t hwork = 0;                   // 16-bit elements
+};
+QrNeed rgsqrf_need(int m, int n, const Options& o);
+
+later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, float* R, int64_t ldr, float* work,
+                      int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
+
+// Split point of a width-n recursion step: the larger half, in 32-column units.
+inline int split_half(int n) { return ((n / 32 + 1) / 2) * 32; }
+
+}  // namespace later

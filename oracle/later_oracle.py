@@ -1,0 +1,148 @@
+"""Numpy restatement of the reference's recursive QR algorithms (CPU oracle).
+
+Test infrastructure only: the CUDA library is checked against this code on the
+same seeded inputs; nothing in the product path imports it.
+
+Precision model (the reference's): matrices are stored in FP32; the trailing
+updates are cublasGemmEx calls on FP16 copies (s2h) with FP32 accumulation,
+restated as FP32 matmuls of FP16-rounded operands (a product of two FP16
+numbers is exact in FP32); panels and their small GEMMs are FP32.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+F32 = np.float32
+
+
+def round16(x: np.ndarray, prec: str = "fp16") -> np.ndarray:
+    """FP32 value of the 16-bit operand the tensor core sees (s2h, util/util.cu:24-32)."""
+    if prec == "fp16":
+        return x.astype(np.float16).astype(F32)
+    if prec == "bf16":
+        # round-to-nearest-even to 8 significand bits
+        u = np.ascontiguousarray(x, dtype=F32).view(np.uint32)
+        r = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+        return r.view(F32).reshape(x.shape)
+    if prec == "split3":
+        hi = x.astype(np.float16).astype(F32)
+        lo = ((x - hi) * F32(2048)).astype(np.float16).astype(F32) / F32(2048)
+        return hi + lo
+    raise ValueError(prec)
+
+
+def tc_gemm(a: np.ndarray, b: np.ndarray, prec: str = "fp16") -> np.ndarray:
+    """FP32-accumulated product of 16-bit-rounded operands (cublasGemmEx, CUDA_R_16F in, CUDA_R_32F out)."""
+    if prec == "split3":
+        ah = a.astype(np.float16).astype(F32)
+        bh = b.astype(np.float16).astype(F32)
+        al = ((a - ah) * F32(2048)).astype(np.float16).astype(F32)
+        bl = ((b - bh) * F32(2048)).astype(np.float16).astype(F32)
+        return (ah @ bh) + (ah @ bl + al @ bh) * F32(1.0 / 2048)
+    return round16(a, prec) @ round16(b, prec)
+
+
+# ------------------------------------------------------------------ panels
+def mgs_block(a: np.ndarray):
+    """MGS of a (<=256) x k block in FP32 — mgs_kernel2, QR/panel.cu:246-325.
+
+    R_kk = ||a_k|| (positive), q_k = a_k / R_kk, then for j > k:
+    R_kj = q_k^T a_j and a_j -= R_kj q_k. Columns beyond the row count are
+    exactly dependent; they are returned as zero columns with a zero R row
+    (the reference leaves them unprocessed, :254,:273).
+    """
+    a = np.array(a, dtype=F32, order="F")
+    mm, k = a.shape
+    r = np.zeros((k, k), dtype=F32)
+    for c in range(k):
+        nrm = F32(np.sqrt(np.dot(a[:, c], a[:, c]))) if c < mm else F32(0)
+        if nrm > 0:
+            a[:, c] *= F32(1) / nrm
+        else:
+            a[:, c] = 0
+        r[c, c] = nrm
+        if c + 1 < k:
+            d = a[:, c] @ a[:, c + 1:]
+            r[c, c + 1:] = d
+            a[:, c + 1:] -= np.outer(a[:, c], d).astype(F32)
+    return a, r
+
+
+def tsqr32(a: np.ndarray, block: int = 256):
+    """TSQR of an m x 32 panel — mgs_caqr_panel_256x32, QR/panel.cu:65-134.
+
+    MGS on each 256-row block, the 32x32 R factors stacked (32 rows per block)
+    and factored recursively, then each block's Q multiplied by its 32x32 slice
+    of the stacked Q (cublasSgemmStridedBatched, :97-102).
+    """
+    m, k = a.shape
+    if m <= block:
+        return mgs_block(a)
+    nb = (m + block - 1) // block
+    q = np.empty_like(a, dtype=F32)
+    stack = np.zeros((nb * k, k), dtype=F32)
+    for i in range(nb):
+        qi, ri = mgs_block(a[i * block:(i + 1) * block])
+        q[i * block:(i + 1) * block] = qi
+        stack[i * k:(i + 1) * k] = ri
+    qs, r = tsqr32(stack, block)
+    for i in range(nb):
+        q[i * block:(i + 1) * block] = q[i * block:(i + 1) * block] @ qs[i * k:(i + 1) * k]
+    return q, r
+
+
+def split_half(n: int) -> int:
+    """Split point of a width-n recursion step (n/2 for the reference's powers of two)."""
+    return ((n // 32 + 1) // 2) * 32
+
+
+def leaf_qr(a: np.ndarray, r: np.ndarray, cgs2: bool = False):
+    """128-wide leaf — mgs_caqr_panel_256x128, QR/panel.cu:10-63: halves down to
+    32-column TSQR panels, glued by FP32 block-CGS updates (cublasSgemm)."""
+    w = a.shape[1]
+    if w <= 32:
+        q, rr = tsqr32(a)
+        a[:] = q
+        r[:w, :w] = rr
+        return
+    w1 = split_half(w)
+    leaf_qr(a[:, :w1], r[:w1, :w1], cgs2)
+    s = a[:, :w1].T @ a[:, w1:]
+    a[:, w1:] -= a[:, :w1] @ s
+    if cgs2:
+        s2 = a[:, :w1].T @ a[:, w1:]
+        a[:, w1:] -= a[:, :w1] @ s2
+        s = s + s2
+    r[:w1, w1:] = s
+    leaf_qr(a[:, w1:], r[w1:, w1:], cgs2)
+
+
+def rgsqrf(A: np.ndarray, leaf: int = 128, prec: str = "fp16", cgs2: bool = False):
+    """Recursive Gram-Schmidt QR — later_rgsqrf / qr, QR/later_rgsqrf.cu:25-79.
+
+    Returns (Q, R) in FP32. Trailing update: R12 = Q1^T A2 (FP16 GemmEx, :45-49),
+    A2 -= Q1 fp16(R12) (:51-56); R12 itself is kept in FP32.
+    """
+    a = np.array(A, dtype=F32, order="F")
+    m, n = a.shape
+    r = np.zeros((n, n), dtype=F32)
+
+    def rec(a, r):
+        nn = a.shape[1]
+        if nn <= leaf:
+            leaf_qr(a, r, cgs2)
+            return
+        n1 = split_half(nn)
+        rec(a[:, :n1], r[:n1, :n1])
+        q1 = a[:, :n1]
+        passes = 2 if cgs2 else 1
+        r12 = np.zeros((n1, nn - n1), dtype=F32)
+        for _ in range(passes):
+            s = tc_gemm(q1.T, a[:, n1:], prec)
+            r12 += s
+            a[:, n1:] -= tc_gemm(q1, s, prec)
+        r[:n1, n1:] = r12
+        rec(a[:, n1:], r[n1:, n1:])
+
+    rec(a, r)
+    return a, r

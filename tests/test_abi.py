@@ -1,0 +1,37 @@
+"""The C-ABI library builds, loads and exports every entry point the headers declare (no GPU needed)."""
+import re
+import subprocess
+from pathlib import Path
+
+import later_gb300 as lg
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared_c_symbols():
+    text = (ROOT / "include" / "later_c.h").read_text()
+    return sorted(set(re.findall(r"\b(later_c_\w+)\s*\(", text)))
+
+
+def test_library_loads_and_exports_c_abi():
+    l = lg.lib()
+    names = _declared_c_symbols()
+    assert names, "no declarations found"
+    for name in names:
+        assert hasattr(l, name), name
+
+
+def test_default_options_and_status_strings():
+    import ctypes
+    l = lg.lib()
+    o = lg.Options()
+    l.later_c_default_options(ctypes.byref(o))
+    assert (o.precision, o.cgs2, o.leaf) == (0, 0, 128)
+    assert l.later_c_status_string(2) == b"workspace too small"
+
+
+def test_bufsize_query_cpu():
+    lw, lh = lg.rgsqrf_bufsize(4096, 1024)
+    assert lh >= 4096 * 1024
+    # The reference test's own work size (test/test_qr.cu:69) is enough to run.
+    assert lw > 0

@@ -1,0 +1,84 @@
+"""Tensor-core GEMM (tcgen05 / TMA / TMEM) against an FP64 product of the same 16-bit operands."""
+import pytest
+import torch
+
+import later_gb300 as lg
+
+pytestmark = pytest.mark.gpu
+
+# Tolerance: FP32 accumulation of K products of 16-bit values; relative to the
+# result's scale. A wrong layout / descriptor gives O(1) errors.
+REL_TOL = 2e-6
+
+
+def _ref(ta, tb, A, B, alpha, beta, C):
+    a = A.double()
+    b = B.double()
+    a = a if ta == "N" else a.t()
+    b = b if tb == "N" else b.t()
+    r = alpha * (a @ b)
+    if C is not None and beta != 0:
+        r = r + beta * C.double()
+    return r
+
+
+def _operand(rows, cols, dt, ld=None, gen=None):
+    x = torch.randn(rows, cols, generator=gen, device="cuda").to(dt)
+    out = lg.empty_colmajor(rows, cols, dtype=dt, ld=ld)
+    out.copy_(x)
+    return out
+
+
+@pytest.mark.parametrize("ta,tb", [("T", "N"), ("N", "N"), ("N", "T"), ("T", "T")])
+@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (256, 256, 256), (200, 136, 72), (384, 64, 1000),
+                                   (1024, 512, 512), (64, 64, 4096)])
+def test_gemm_layouts(cuda, ta, tb, m, n, k):
+    g = torch.Generator(device="cuda").manual_seed(m * 7 + n * 3 + k)
+    A = _operand(m if ta == "N" else k, k if ta == "N" else m, torch.float16, gen=g)
+    B = _operand(k if tb == "N" else n, n if tb == "N" else k, torch.float16, gen=g)
+    D = lg.gemm16(ta, tb, A, B)
+    assert lg.device_status() == 0
+    ref = _ref(ta, tb, A, B, 1.0, 0.0, None)
+    err = (D.double() - ref).norm() / ref.norm()
+    assert err < REL_TOL, float(err)
+
+
+@pytest.mark.parametrize("prec,dt", [("fp16", torch.float16), ("bf16", torch.bfloat16)])
+def test_gemm_alpha_beta_inplace(cuda, prec, dt):
+    m, n, k = 640, 384, 320
+    g = torch.Generator(device="cuda").manual_seed(5)
+    A = _operand(m, k, dt, gen=g)
+    B = _operand(k, n, dt, gen=g)
+    C = lg.colmajor(torch.randn(m, n, generator=g, device="cuda"))
+    ref = _ref("N", "N", A, B, -1.0, 1.0, C)
+    lg.gemm16("N", "N", A, B, alpha=-1.0, beta=1.0, C=C, D=C, precision=prec)
+    assert lg.device_status() == 0
+    err = (C.double() - ref).norm() / ref.norm()
+    assert err < REL_TOL, float(err)
+
+
+def test_gemm_splitk_deterministic(cuda):
+    # Small output, long K: exercises the split-K partial tiles + ticketed reduction.
+    m, n, k = 256, 256, 16384
+    g = torch.Generator(device="cuda").manual_seed(11)
+    A = _operand(k, m, torch.float16, gen=g)
+    B = _operand(k, n, torch.float16, gen=g)
+    work = torch.empty(1 << 24, dtype=torch.float32, device="cuda")
+    D1 = lg.gemm16("T", "N", A, B, work=work)
+    D2 = lg.gemm16("T", "N", A, B, work=work)
+    assert lg.device_status() == 0
+    ref = _ref("T", "N", A, B, 1.0, 0.0, None)
+    err = (D1.double() - ref).norm() / ref.norm()
+    assert err < REL_TOL, float(err)
+    assert torch.equal(D1, D2)
+
+
+def test_gemm_leading_dims(cuda):
+    m, n, k = 300, 200, 136
+    g = torch.Generator(device="cuda").manual_seed(3)
+    A = _operand(k, m, torch.float16, ld=k + 24, gen=g)
+    B = _operand(k, n, torch.float16, ld=k + 8, gen=g)
+    D = lg.empty_colmajor(m, n, ld=m + 5)
+    lg.gemm16("T", "N", A, B, D=D)
+    ref = _ref("T", "N", A, B, 1.0, 0.0, None)
+    assert (D.double() - ref).norm() / ref.norm() < REL_TOL
