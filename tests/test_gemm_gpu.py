@@ -6,9 +6,10 @@ import later_gb300 as lg
 
 pytestmark = pytest.mark.gpu
 
-# Tolerance: FP32 accumulation of K products of 16-bit values; relative to the
-# result's scale. A wrong layout / descriptor gives O(1) errors.
-REL_TOL = 2e-6
+# Tolerance: FP32 accumulation of K exact products of 16-bit values; the
+# rounding error grows like sqrt(K) u32. A wrong layout / descriptor gives O(1).
+def rel_tol(k):
+    return 1e-6 + 2e-7 * k ** 0.5
 
 
 def _ref(ta, tb, A, B, alpha, beta, C):
@@ -40,7 +41,7 @@ def test_gemm_layouts(cuda, ta, tb, m, n, k):
     assert lg.device_status() == 0
     ref = _ref(ta, tb, A, B, 1.0, 0.0, None)
     err = (D.double() - ref).norm() / ref.norm()
-    assert err < REL_TOL, float(err)
+    assert err < rel_tol(k), float(err)
 
 
 @pytest.mark.parametrize("prec,dt", [("fp16", torch.float16), ("bf16", torch.bfloat16)])
@@ -54,7 +55,7 @@ def test_gemm_alpha_beta_inplace(cuda, prec, dt):
     lg.gemm16("N", "N", A, B, alpha=-1.0, beta=1.0, C=C, D=C, precision=prec)
     assert lg.device_status() == 0
     err = (C.double() - ref).norm() / ref.norm()
-    assert err < REL_TOL, float(err)
+    assert err < rel_tol(k), float(err)
 
 
 def test_gemm_splitk_deterministic(cuda):
@@ -69,7 +70,7 @@ def test_gemm_splitk_deterministic(cuda):
     assert lg.device_status() == 0
     ref = _ref("T", "N", A, B, 1.0, 0.0, None)
     err = (D1.double() - ref).norm() / ref.norm()
-    assert err < REL_TOL, float(err)
+    assert err < rel_tol(k), float(err)
     assert torch.equal(D1, D2)
 
 
@@ -81,4 +82,4 @@ def test_gemm_leading_dims(cuda):
     D = lg.empty_colmajor(m, n, ld=m + 5)
     lg.gemm16("T", "N", A, B, D=D)
     ref = _ref("T", "N", A, B, 1.0, 0.0, None)
-    assert (D.double() - ref).norm() / ref.norm() < REL_TOL
+    assert (D.double() - ref).norm() / ref.norm() < rel_tol(k)
