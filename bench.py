@@ -1,0 +1,337 @@
+"""Benchmark: recursive tensor-core QR (later_rgsqrf) on one GB300.
+
+Workload (default): rgsqrf of a 16384 x 16384 FP32 matrix, entries N(0,1)
+from a fixed seed, FP16 tensor-core trailing updates with FP32 accumulation,
+leaf panel width 128 — the square shape of the QR precision sweep. The metric
+is the reference's QR rate, 2 n^2 (m - n/3) / t (test/test_qr.cu:85-86), in
+TFLOP/s, reported beside the backward error ||A - QR|| / ||A||.
+
+A step is one QR of the full matrix. The matrix (1 GiB) is larger than L2, and
+it is restored from a pristine device copy before each step (outside the
+per-step events). `value` is the device-timed rate with inputs resident in
+HBM; `e2e` is the same QR through the public API with the matrix copied from
+pinned host memory and Q and R copied back inside the timed region.
+
+--impl reference times the reference algorithm on the host cores: the
+oracle's numpy restatement of later_rgsqrf (no GPU), on a bounded sample.
+
+Multi-GPU: a single QR does not shard (replicas only); under torchrun every
+rank factors its own matrix and `value` sums the ranks' rates (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "QR TFLOP/s (LAPACK count 2n^2(m-n/3)) at stated ||A-QR||/||A||"
+
+
+def qr_flops(m, n):
+    return 2.0 * n * n * (m - n / 3.0)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--m", type=int, default=16384)
+    p.add_argument("--n", type=int, default=16384)
+    p.add_argument("--precision", default="fp16", choices=["fp16", "bf16", "split3"])
+    p.add_argument("--leaf", type=int, default=128)
+    p.add_argument("--cgs2", action="store_true")
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    p.add_argument("--cpu-m", type=int, default=16384, help="CPU sample rows")
+    p.add_argument("--cpu-n", type=int, default=1024, help="CPU sample columns")
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------ CPU baselines
+def cpu_oracle_rate(m, n, seed, threads=None):
+    """Times the oracle restatement of later_rgsqrf (numpy, all host threads) on an m x n sample."""
+    import numpy as np
+    from oracle import gen
+    from oracle import later_oracle as lo
+    A = gen.normal(m, n, seed)
+    lo.rgsqrf(A[: min(m, 2048), : min(n, 256)])  # warm-up (BLAS threads, caches)
+    t = time.perf_counter()
+    lo.rgsqrf(A)
+    dt = time.perf_counter() - t
+    return qr_flops(m, n) / dt / 1e12, dt
+
+
+def host_sgeqrf_rate(m, n, seed):
+    """Host LAPACK sgeqrf (scipy's bundled OpenBLAS, all host cores) on an m x n sample."""
+    try:
+        import scipy.linalg.lapack as la
+    except Exception:
+        return None, None
+    from oracle import gen
+    A = gen.normal(m, n, seed)
+    la.sgeqrf(A[:1024, :256].copy(order="F"))
+    t = time.perf_counter()
+    la.sgeqrf(A, overwrite_a=True)
+    dt = time.perf_counter() - t
+    return qr_flops(m, n) / dt / 1e12, dt
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return
+    ncores = os.cpu_count() or 1
+    rates = []
+    for _ in range(a.warmup):
+        cpu_oracle_rate(a.cpu_m, a.cpu_n, a.seed)
+    for _ in range(a.steps):
+        r, _ = cpu_oracle_rate(a.cpu_m, a.cpu_n, a.seed)
+        rates.append(r)
+    v = statistics.median(rates)
+    sample = f"oracle restatement of later_rgsqrf (numpy, fp16-rounded GEMM operands) on {a.cpu_m}x{a.cpu_n}, N(0,1) seed {a.seed}"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": qr_flops(a.cpu_m, a.cpu_n) / v / 1e9,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": a.precision,
+            "data": "synthetic", "config": workload_config(a),
+            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": ncores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(a):
+    return {"workload": f"rgsqrf {a.m}x{a.n} fp32, N(0,1) seed {a.seed}, {a.precision} tensor-core trailing "
+                        f"updates, leaf {a.leaf}{', CGS2' if a.cgs2 else ''}",
+            "m": a.m, "n": a.n, "precision": a.precision, "leaf": a.leaf, "cgs2": a.cgs2,
+            "l2": "inputs larger than L2 (matrix >= 1 GiB at the default size)"}
+
+
+# ------------------------------------------------------------------ ours
+def run_ours(a, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    import later_gb300 as lg
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    m, n = a.m, a.n
+    flops = qr_flops(m, n)
+    g = torch.Generator(device=dev).manual_seed(a.seed + rank)
+    A0 = torch.randn(n, m, generator=g, device=dev).t()  # column-major m x n
+    A = lg.empty_colmajor(m, n, device=dev)
+    R = lg.empty_colmajor(n, n, device=dev)
+    lw, lh = lg.rgsqrf_bufsize(m, n, a.precision, a.cgs2, a.leaf)
+    work = torch.empty(lw, dtype=torch.float32, device=dev)
+    hwork = torch.empty(lh, dtype=torch.float16, device=dev)
+    st = torch.cuda.current_stream()
+
+    def qr():
+        lg.later_rgsqrf(A, R, work, hwork, precision=a.precision, cgs2=a.cgs2, leaf=a.leaf)
+
+    for _ in range(a.warmup):
+        A.copy_(A0)
+        qr()
+    status = lg.device_status()
+    if status != 0:
+        raise RuntimeError(f"device status {status} during warm-up")
+
+    # ---- timed region (device events per step; restore copy outside the events)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = lg.launch_count()
+    evs = []
+    with ClockSampler(local_rank) as clk:
+        t_wall = time.perf_counter()
+        for _ in range(a.steps):
+            A.copy_(A0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            qr()
+            e1.record(st)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    if world > 1:
+        dist.barrier()
+    launches = lg.launch_count() - launches0
+    ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    ms_step = sum(ms) / len(ms)
+    clocks = clk.summary()
+
+    # ---- accuracy of the last step (FP32 on the GPU, TF32 off, like the reference's checker)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    Rt = torch.triu(R)
+    res = (A0 - A @ Rt).norm() / A0.norm()
+    eye = torch.eye(n, device=dev)
+    orth = (eye - A.t() @ A).norm()
+    bwd, orth = float(res), float(orth)
+
+    # ---- per-class trace of one extra step (roofline of the dominant kernel)
+    A.copy_(A0)
+    lg.trace_begin()
+    qr()
+    tr = lg.trace_end()
+
+    # ---- end to end through the public API: pinned host A in, Q and R out
+    e2e = None
+    if a.e2e_steps > 0:
+        hA = A0.cpu().pin_memory()
+        hQ = torch.empty(n, m, pin_memory=True).t()
+        hR = torch.empty(n, n, pin_memory=True).t()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(a.e2e_steps):
+            A.copy_(hA, non_blocking=True)
+            qr()
+            hQ.copy_(A, non_blocking=True)
+            hR.copy_(R, non_blocking=True)
+        e1.record(st)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1) / a.e2e_steps
+        e2e = {"value": flops / e2e_ms / 1e9, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
+               "h2d_bytes_per_step": m * n * 4, "d2h_bytes_per_step": m * n * 4 + n * n * 4}
+
+    # ---- aggregate over ranks (max time)
+    rate = flops / ms_step / 1e9
+    if world > 1:
+        t = torch.tensor([ms_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t)
+        value = world * flops / ms_max / 1e9
+    else:
+        ms_max = ms_step
+        value = rate
+    if rank != 0:
+        return
+
+    import json as _j
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = _j.loads(pk.read_text())
+    peak = peaks.get("bf16_tflops")
+    peak_src = "measured bf16 burst (MEASURED_PEAKS.json)" if peak else "fallback 1900 TFLOP/s"
+    peak = peak or 1900.0
+    top_ach = tr["top_gemm_flops"] / tr["top_gemm_ms"] / 1e9 if tr["top_gemm_ms"] else None
+    all_ach = tr["gemm_flops"] / tr["gemm_ms"] / 1e9 if tr["gemm_ms"] else None
+    roof = {"bound": "tensor", "kernel": "tc_gemm_kernel (largest launch: top-level trailing update)",
+            "achieved": top_ach, "peak": peak, "unit": "TFLOP/s", "frac": (top_ach / peak) if top_ach else None,
+            "peak_source": peak_src, "traffic": None,
+            "all_gemm_achieved": all_ach, "all_gemm_frac": (all_ach / peak) if all_ach else None}
+
+    cpu = None
+    if not a.no_cpu:
+        r_or, dt_or = cpu_oracle_rate(a.cpu_m, a.cpu_n, a.seed)
+        r_la, dt_la = host_sgeqrf_rate(a.cpu_m, a.cpu_n, a.seed)
+        cpu = {"value": r_or, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"oracle restatement of later_rgsqrf (numpy, all host threads) on {a.cpu_m}x{a.cpu_n} "
+                         f"N(0,1), {dt_or:.2f} s",
+               "host_sgeqrf": {"value": r_la, "unit": "TFLOP/s", "seconds": dt_la,
+                               "sample": f"scipy OpenBLAS sgeqrf {a.cpu_m}x{a.cpu_n}"}}
+
+    line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": a.precision, "data": "synthetic",
+            "config": workload_config(a),
+            "accuracy": {"backward_error": bwd, "orthogonality_fro": orth, "orthogonality_over_n": orth / n,
+                         "computed": "FP32 on GPU, TF32 off (as test/test_qr.cu:216-268)"},
+            "executed_tflops": 2.0 * m * n * n / ms_step / 1e9,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "launches_per_step": launches / max(1, a.steps), "clocks": clocks,
+            "wall_s_timed_region": t_wall,
+            "trace_ms": {"gemm": tr["gemm_ms"], "panel": tr["panel_ms"], "leaf_gemm": tr["leaf_gemm_ms"],
+                         "other": tr["other_ms"]}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    try:
+        run_ours(a, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -99,6 +99,31 @@ later_status_t later_c_gemm16(later_stream_t stream, char transa, char transb, i
 later_status_t later_c_convert(later_stream_t stream, int m, int n, const float* A, int lda, void* hi,
                                void* lo, int ldh, int precision);
 
+/* ------------------------------------------------------------ tracing */
+
+/* Cumulative number of kernels this library has launched (all streams). */
+uint64_t later_c_launch_count(void);
+
+typedef struct {
+  double gemm_flops;      /* algorithmic flops (2 m n k) of the tensor-core GEMMs */
+  double gemm_ms;         /* their summed device time */
+  int64_t gemm_launches;
+  double top_gemm_flops;  /* the largest single GEMM launch ... */
+  double top_gemm_ms;     /* ... and its device time */
+  double panel_ms;        /* FP32 TSQR panels (reduction tree + apply) */
+  int64_t panel_launches;
+  double leaf_gemm_flops; /* FP32 leaf projections */
+  double leaf_gemm_ms;
+  int64_t leaf_gemm_launches;
+  double other_ms;        /* conversions, fills, small solves */
+  int64_t other_launches;
+} later_trace_t;
+
+/* Starts event tracing of every launch group on its stream (clears old records). */
+void later_c_trace_begin(void);
+/* Stops tracing, waits for the recorded events and returns the per-class sums. */
+later_status_t later_c_trace_end(later_trace_t* out);
+
 #ifdef __cplusplus
 }
 #endif

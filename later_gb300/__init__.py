@@ -19,7 +19,8 @@ from . import build as _build
 
 __all__ = [
     "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
-    "later_rgsqrf", "rgsqrf_bufsize", "gemm16", "convert16", "device_status",
+    "later_rgsqrf", "rgsqrf_bufsize", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
+    "trace_end",
 ]
 
 PREC = {"fp16": 0, "bf16": 1, "split3": 2}
@@ -55,7 +56,22 @@ _SIGS = {
     "later_c_gemm16": (_i, [_vp, ctypes.c_char, ctypes.c_char, _i, _i, _i, _f, _vp, _i, _vp, _i, _f, _vp, _i,
                             _vp, _i, _i, _vp, _i64]),
     "later_c_convert": (_i, [_vp, _i, _i, _vp, _i, _vp, _vp, _i, _i]),
+    "later_c_launch_count": (ctypes.c_uint64, []),
+    "later_c_trace_begin": (None, []),
+    "later_c_trace_end": (_i, [_vp]),
 }
+
+
+class Trace(ctypes.Structure):
+    _fields_ = [("gemm_flops", ctypes.c_double), ("gemm_ms", ctypes.c_double), ("gemm_launches", ctypes.c_int64),
+                ("top_gemm_flops", ctypes.c_double), ("top_gemm_ms", ctypes.c_double),
+                ("panel_ms", ctypes.c_double), ("panel_launches", ctypes.c_int64),
+                ("leaf_gemm_flops", ctypes.c_double), ("leaf_gemm_ms", ctypes.c_double),
+                ("leaf_gemm_launches", ctypes.c_int64), ("other_ms", ctypes.c_double),
+                ("other_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 def lib_path() -> Path:
@@ -113,6 +129,21 @@ def _check(status: int, where: str):
 def device_status(stream=None) -> int:
     """Synchronises the stream and returns (and clears) the device status word."""
     return lib().later_c_device_status(_stream(stream))
+
+
+def launch_count() -> int:
+    """Cumulative number of kernels the library has launched."""
+    return int(lib().later_c_launch_count())
+
+
+def trace_begin():
+    lib().later_c_trace_begin()
+
+
+def trace_end() -> dict:
+    t = Trace()
+    _check(lib().later_c_trace_end(ctypes.byref(t)), "trace_end")
+    return t.as_dict()
 
 
 def rgsqrf_bufsize(m, n, precision="fp16", cgs2=False, leaf=128):

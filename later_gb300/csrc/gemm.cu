@@ -69,6 +69,30 @@ __device__ __forceinline__ void store16(void* base, int64_t idx, float v, int bf
     reinterpret_cast<__half*>(base)[idx] = __float2half_rn(v);
 }
 
+// Epilogue of one output element: D = alpha*acc + beta*C, plus the 16-bit copy.
+// `c` is the already-loaded C element (ignored when beta == 0).
+__device__ __forceinline__ void epilogue_store_c(const GemmArgs& p, int row, int col, float acc, float c) {
+  if (row >= p.M || col >= p.N) return;
+  if (p.lower && row < col + p.diag) return;
+  const float prod = p.alpha * acc;
+  float v = prod;
+  if (p.beta != 0.f) v += p.beta * c;
+  p.D[row + static_cast<int64_t>(col) * p.ldd] = v;
+  if (p.Dh) {
+    if (p.shadow_acc) v = prod;
+    const int64_t hidx = row + static_cast<int64_t>(col) * p.ldh;
+    if (p.out_mode == 1) {
+      store16(p.Dh, hidx, v, 1);
+    } else {
+      if (fabsf(v) > 65504.f) report(p.status, DEV_RANGE);
+      const __half h = __float2half_rn(v);
+      reinterpret_cast<__half*>(p.Dh)[hidx] = h;
+      if (p.out_mode == 2)
+        reinterpret_cast<__half*>(p.Dl)[hidx] = __float2half_rn((v - __half2float(h)) * kLoScale);
+    }
+  }
+}
+
 template <int BN, bool A_MN, bool B_MN, bool SPLIT, int STAGES>
 struct Cfg {
   static constexpr int A_BYTES = BM * BK * 2;  // 16 KB
@@ -216,86 +240,75 @@ __global__ void __launch_bounds__(128, 1)
   const int r = warp * 32 + lane;  // tile row == TMEM lane
   const int row = m0 + r;
   const uint32_t t_row = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-  const int out16 = (p.Dh != nullptr);
-
-  auto finish = [&](int col, float acc) {
-    if (row >= p.M || col >= p.N) return;
-    if (p.lower && row < col + p.diag) return;
-    const float prod = p.alpha * acc;
-    float v = prod;
-    if (p.beta != 0.f) v += p.beta * p.C[row + static_cast<int64_t>(col) * p.ldc];
-    p.D[row + static_cast<int64_t>(col) * p.ldd] = v;
-    if (out16) {
-      if (p.shadow_acc) v = prod;
-      const int64_t hidx = row + static_cast<int64_t>(col) * p.ldh;
-      if (p.out_mode == 1) {
-        store16(p.Dh, hidx, v, 1);
-      } else {
-        if (fabsf(v) > 65504.f) report(p.status, DEV_RANGE);
-        const __half h = __float2half_rn(v);
-        reinterpret_cast<__half*>(p.Dh)[hidx] = h;
-        if (p.out_mode == 2)
-          reinterpret_cast<__half*>(p.Dl)[hidx] = __float2half_rn((v - __half2float(h)) * kLoScale);
-      }
-    }
-  };
-
-  if (p.splits == 1) {
+  // Split-K: this CTA's FP32 partial tile, [col][row], reduced by splitk_reduce_kernel.
+  float* mine = p.splits > 1 ? p.partial + (static_cast<int64_t>(blockIdx.x) * p.splits + split) * (BM * BN)
+                             : nullptr;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      float v[32];
-      tmem_ld_32x32b_x32(t_row + c0, v);
-      if (SPLIT) {
-        float w[32];
-        tmem_ld_32x32b_x32(t_row + BN + c0, w);
+  for (int c0 = 0; c0 < BN; c0 += 32) {
+    float v[32];
+    tmem_ld_32x32b_x32(t_row + c0, v);
+    if (SPLIT) {
+      float w[32];
+      tmem_ld_32x32b_x32(t_row + BN + c0, w);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] += w[j] * kLoScaleInv;
-      }
-      if (ok) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) finish(n0 + c0 + j, v[j]);
-      }
+      for (int j = 0; j < 32; ++j) v[j] += w[j] * kLoScaleInv;
     }
-  } else {
-    const int tile = blockIdx.x;
-    float* mine = p.partial + (static_cast<int64_t>(tile) * p.splits + split) * (BM * BN);
-#pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      float v[32];
-      tmem_ld_32x32b_x32(t_row + c0, v);
-      if (SPLIT) {
-        float w[32];
-        tmem_ld_32x32b_x32(t_row + BN + c0, w);
-#pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] += w[j] * kLoScaleInv;
-      }
+    if (mine) {
 #pragma unroll
       for (int j = 0; j < 32; ++j) __stcg(&mine[(c0 + j) * BM + r], ok ? v[j] : 0.f);
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const int prev = atomicAdd(&p.counters[tile], 1);
-      *last_flag = (prev == p.splits - 1) ? 1 : 0;
-    }
-    __syncthreads();
-    if (*last_flag) {
-      __threadfence();
-      const float* base = p.partial + static_cast<int64_t>(tile) * p.splits * (BM * BN);
-#pragma unroll 1
-      for (int c = 0; c < BN; ++c) {
-        float acc = 0.f;
-#pragma unroll 1
-        for (int s = 0; s < p.splits; ++s) acc += __ldcg(&base[static_cast<int64_t>(s) * (BM * BN) + c * BM + r]);
-        finish(n0 + c, acc);
+    } else if (ok) {
+      // C and D may alias: read the chunk's 32 C values before any store so the
+      // loads overlap instead of serialising behind the stores.
+      float cv[32];
+      const bool rd = (p.beta != 0.f) && row < p.M;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int col = n0 + c0 + j;
+        cv[j] = (rd && col < p.N) ? p.C[row + static_cast<int64_t>(col) * p.ldc] : 0.f;
       }
-      if (threadIdx.x == 0) p.counters[tile] = 0;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) epilogue_store_c(p, row, n0 + c0 + j, v[j], cv[j]);
     }
   }
 
   tc_fence_before();
   __syncthreads();
   if (warp == 1) tmem_dealloc(tmem, C_::TMEM_COLS);
+}
+
+// Deterministic split-K reduction: 256 threads = 32 rows x 8 slices; slice j
+// sums partials j, j+8, ... in order, then the 8 slice sums are combined in a
+// fixed tree. One block covers 32 rows x 4 columns of one tile.
+template <int BN>
+__global__ void __launch_bounds__(256) splitk_reduce_kernel(const GemmArgs p) {
+  __shared__ float part[8][4][33];
+  const int tiles_per_row_groups = (BM / 32) * (BN / 4);
+  const int tile = blockIdx.x / tiles_per_row_groups;
+  const int rem = blockIdx.x % tiles_per_row_groups;
+  const int rg = rem % (BM / 32);
+  const int cg = rem / (BM / 32);
+  const int tile_m = tile % p.tiles_m, tile_n = tile / p.tiles_m;
+  const int r = rg * 32 + threadIdx.x % 32;
+  const int j = threadIdx.x / 32;
+  const float* base = p.partial + static_cast<int64_t>(tile) * p.splits * (BM * BN);
+#pragma unroll
+  for (int cc = 0; cc < 4; ++cc) {
+    const int c = cg * 4 + cc;
+    float acc = 0.f;
+#pragma unroll 8
+    for (int s = j; s < p.splits; s += 8) acc += __ldcg(&base[static_cast<int64_t>(s) * (BM * BN) + c * BM + r]);
+    part[j][cc][threadIdx.x % 32] = acc;
+  }
+  __syncthreads();
+  if (j < 4) {
+    const int cc = j;
+    const int l = threadIdx.x % 32;
+    const float v = ((part[0][cc][l] + part[1][cc][l]) + (part[2][cc][l] + part[3][cc][l])) +
+                    ((part[4][cc][l] + part[5][cc][l]) + (part[6][cc][l] + part[7][cc][l]));
+    const int row = tile_m * BM + r, col = tile_n * BN + cg * 4 + cc;
+    const float c = (p.beta != 0.f && row < p.M && col < p.N) ? p.C[row + static_cast<int64_t>(col) * p.ldc] : 0.f;
+    epilogue_store_c(p, row, col, v, c);
+  }
 }
 
 // ------------------------------------------------------------------- host
@@ -326,7 +339,15 @@ later_status_t launch_cfg(const CUtensorMap& a, const CUtensorMap& b, const CUte
     attr_done[dev] = true;
   }
   kern<<<grid, 128, C_::SMEM, st>>>(a, b, al, bl, args);
-  return cuda_status(cudaGetLastError());
+  note_launch();
+  LATER_CHECK_CUDA(cudaGetLastError());
+  if (args.splits > 1) {
+    const int blocks = static_cast<int>(grid.x) * (BM / 32) * (BN / 4);
+    splitk_reduce_kernel<BN><<<blocks, 256, 0, st>>>(args);
+    note_launch();
+    LATER_CHECK_CUDA(cudaGetLastError());
+  }
+  return LATER_OK;
 }
 
 template <int BN, bool SPLIT, int STAGES>
@@ -435,6 +456,7 @@ later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, lon
   }
 
   dim3 grid(tiles, splits);
+  TraceScope trace(st, TRACE_GEMM, 2.0 * g.M * g.N * static_cast<double>(g.K));
   if (split3) {
     if (BN == 64) return launch_bn<64, true, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
     return launch_bn<128, true, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);

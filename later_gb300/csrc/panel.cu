@@ -8,10 +8,10 @@
 // FP32 cublasSgemm block-CGS updates (QR/panel.cu:10-63).
 //
 // Here the whole reduction tree is one launch (tsqr_reduce_kernel): every CTA
-// factors its 256 x 32 block with MGS held in registers (warp = column,
-// 8 rows per lane), writes Q in place and its R into the next level's stack,
-// then takes an atomic ticket; the last CTA of each group of eight carries on
-// with the next level, so no CTA ever waits on another. A second launch
+// factors its 256-row block with MGS held in registers (warp = column),
+// writes Q in place and its R into the next level's stack, then takes an
+// atomic ticket; the last CTA of each group of eight carries on with the next
+// level, so no CTA ever waits on another CTA. A second launch
 // (tsqr_apply_kernel) composes each block's path through the tree (32x32
 // products) and writes the final Q in FP32 together with its 16-bit copy, so
 // the tensor-core GEMMs that follow need no conversion pass.
@@ -20,15 +20,18 @@
 #include <cuda_runtime.h>
 
 #include "panel.cuh"
+#include "ptx.cuh"
 #include "runtime.cuh"
 
 namespace later {
 
 namespace {
 
-constexpr int PB = 32;    // panel width
-constexpr int BR = 256;   // rows per TSQR block
-constexpr int RPL = BR / 32;  // rows per lane
+constexpr int PB = 32;       // panel width
+constexpr int BR = 256;      // rows per TSQR block at every level
+constexpr int RPL = BR / 32; // rows per lane
+constexpr int kGroup = BR / PB;  // blocks of one level stacked into a block of the next (8)
+constexpr int APPLY_ROWS = 256;
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -36,21 +39,31 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-// MGS of one (<=256) x 32 block held in registers. Warp w owns column w; lane
-// l holds rows l + 32 t. q buffers are double-buffered so each step needs one
-// barrier. Columns beyond the block's row count are exactly dependent and are
-// set to zero (R row zero) instead of normalising round-off.
-__device__ void mgs_block(float (&a)[RPL], int mm, float* qbuf /*2*BR*/, float* Rs /*32x33*/) {
+// MGS of one (<= 256) x 32 block held in registers: warp w owns column w,
+// lane l holds rows l + 32 t. One barrier per step (q_k is double-buffered in
+// shared memory). Squared column norms are downdated by Pythagoras
+// (s -= d^2) after each projection, so the critical path of a step has one
+// warp reduction; when a column has lost more than half of its squared norm
+// the norm is recomputed exactly (no cancellation). Columns beyond the
+// block's row count are exactly dependent: q = 0, zero R row.
+__device__ void mgs_block(float (&a)[RPL], int mm, float* qbuf /*2 x 256*/, float* Rs /*32 x 33*/) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  float s0 = 0.f;
+#pragma unroll
+  for (int t = 0; t < RPL; ++t) s0 += a[t] * a[t];
+  s0 = warp_sum(s0);
+  float s = s0;
 #pragma unroll 1
   for (int k = 0; k < PB; ++k) {
     float* q = qbuf + (k & 1) * BR;
     if (w == k) {
-      float s = 0.f;
+      if (!(s > 0.5f * s0)) {
+        s = 0.f;
 #pragma unroll
-      for (int t = 0; t < RPL; ++t) s += a[t] * a[t];
-      s = warp_sum(s);
-      float nrm = sqrtf(s);
+        for (int t = 0; t < RPL; ++t) s += a[t] * a[t];
+        s = warp_sum(s);
+      }
+      float nrm = sqrtf(fmaxf(s, 0.f));
       if (k >= mm || !(nrm > 0.f)) nrm = 0.f;
       const float inv = nrm > 0.f ? 1.f / nrm : 0.f;
 #pragma unroll
@@ -62,18 +75,26 @@ __device__ void mgs_block(float (&a)[RPL], int mm, float* qbuf /*2*BR*/, float* 
     }
     __syncthreads();
     if (w > k) {
+      float qv[RPL];
       float d = 0.f;
 #pragma unroll
-      for (int t = 0; t < RPL; ++t) d += q[l + 32 * t] * a[t];
+      for (int t = 0; t < RPL; ++t) {
+        qv[t] = q[l + 32 * t];
+        d += qv[t] * a[t];
+      }
       d = warp_sum(d);
 #pragma unroll
-      for (int t = 0; t < RPL; ++t) a[t] -= d * q[l + 32 * t];
-      if (l == 0) Rs[k * 33 + w] = d;  // Rs[row k][col w]
+      for (int t = 0; t < RPL; ++t) a[t] -= d * qv[t];
+      s -= d * d;
+      if (l == 0) Rs[k * 33 + w] = d;  // R[k][w]
     }
   }
   __syncthreads();
 }
 
+// Whole TSQR reduction tree in one launch. Each CTA factors one level-0 block;
+// the last CTA of each group (atomic ticket) factors the group's stacked R at
+// the next level, and so on up to the root. Q factors stay in place.
 __global__ void __launch_bounds__(1024, 1) tsqr_reduce_kernel(TsqrPlan P) {
   __shared__ float qbuf[2 * BR];
   __shared__ float Rs[PB * 33];
@@ -84,9 +105,8 @@ __global__ void __launch_bounds__(1024, 1) tsqr_reduce_kernel(TsqrPlan P) {
   while (true) {
     float* X = P.lev[L];
     const int64_t ld = P.ld[L];
-    const int rows = P.rows[L];
     const int r0 = b * BR;
-    const int mm = min(BR, rows - r0);
+    const int mm = min(BR, P.rows[L] - r0);
     float a[RPL];
 #pragma unroll
     for (int t = 0; t < RPL; ++t) {
@@ -94,26 +114,21 @@ __global__ void __launch_bounds__(1024, 1) tsqr_reduce_kernel(TsqrPlan P) {
       a[t] = (r < mm) ? __ldcg(&X[r0 + r + static_cast<int64_t>(w) * ld]) : 0.f;
     }
     mgs_block(a, mm, qbuf, Rs);
-    // Q in place.
 #pragma unroll
     for (int t = 0; t < RPL; ++t) {
       const int r = l + 32 * t;
       if (r < mm) X[r0 + r + static_cast<int64_t>(w) * ld] = a[t];
     }
-    // R: to the output at the root, else into the next level's stack.
     const bool root = (P.nblk[L] == 1);
     float* Ro = root ? P.R : P.lev[L + 1] + 32 * b;
     const int64_t ldo = root ? P.ldr : P.ld[L + 1];
-    {
-      const int i = l, j = w;  // element (i, j) of the 32x32 R
-      Ro[i + static_cast<int64_t>(j) * ldo] = (i <= j) ? Rs[i * 33 + j] : 0.f;
-    }
+    Ro[l + static_cast<int64_t>(w) * ldo] = (l <= w) ? Rs[l * 33 + w] : 0.f;
     if (root) break;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-      const int g = b >> 3;
-      const int gsize = min(8, P.nblk[L] - 8 * g);
+      const int g = b / kGroup;
+      const int gsize = min(kGroup, P.nblk[L] - kGroup * g);
       int* c = P.counters + P.cnt_off[L] + g;
       const int prev = atomicAdd(c, 1);
       last = (prev == gsize - 1);
@@ -122,7 +137,7 @@ __global__ void __launch_bounds__(1024, 1) tsqr_reduce_kernel(TsqrPlan P) {
     __syncthreads();
     if (!last) break;
     __threadfence();
-    b >>= 3;
+    b /= kGroup;
     ++L;
   }
 }
@@ -133,35 +148,47 @@ __global__ void __launch_bounds__(256) tsqr_apply_kernel(TsqrPlan P, void* qh, v
                                                          int out_mode) {
   __shared__ float T[PB * 33];
   __shared__ float U[PB * 33];
-  const int b = blockIdx.x;
+  const int row0 = blockIdx.x * APPLY_ROWS;
+  const int b = row0 / P.br[0];  // level-0 block
   const int tid = threadIdx.x;
   const int top = P.nlev - 1;
-  // T = slice of the top level, then T = slice_L * T down to level 1.
+  // Index at level L of the level-0 block b: b / div[L].
   if (top == 0) {
     for (int e = tid; e < PB * PB; e += 256) T[(e % PB) * 33 + e / PB] = (e % PB == e / PB) ? 1.f : 0.f;
   } else {
-    const int bt = b >> (3 * (top - 1));  // block index at level top-1
+    const int bt = b / P.div[top - 1];  // block index at level top-1
     for (int e = tid; e < PB * PB; e += 256) {
       const int i = e % PB, j = e / PB;
       T[i * 33 + j] = __ldcg(&P.lev[top][32 * bt + i + static_cast<int64_t>(j) * P.ld[top]]);
     }
     for (int L = top - 1; L >= 1; --L) {
       __syncthreads();
-      const int bl = b >> (3 * (L - 1));
-      for (int e = tid; e < PB * PB; e += 256) {
+      const int bl = b / P.div[L - 1];
+      for (int e = tid; e < PB * PB; e += 256) {  // stage the 32x32 slice
         const int i = e % PB, j = e / PB;
-        float s = 0.f;
-#pragma unroll 8
-        for (int k = 0; k < PB; ++k)
-          s += __ldcg(&P.lev[L][32 * bl + i + static_cast<int64_t>(k) * P.ld[L]]) * T[k * 33 + j];
-        U[i * 33 + j] = s;
+        U[i * 33 + j] = __ldcg(&P.lev[L][32 * bl + i + static_cast<int64_t>(j) * P.ld[L]]);
       }
       __syncthreads();
-      for (int e = tid; e < PB * PB; e += 256) T[(e % PB) * 33 + e / PB] = U[(e % PB) * 33 + e / PB];
+      float out[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = tid + 256 * u;
+        const int i = e % PB, j = e / PB;
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k < PB; ++k) acc += U[i * 33 + k] * T[k * 33 + j];
+        out[u] = acc;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = tid + 256 * u;
+        T[(e % PB) * 33 + e / PB] = out[u];
+      }
     }
   }
   __syncthreads();
-  const int row = b * BR + tid;
+  const int row = row0 + tid;
   if (row >= P.rows[0]) return;
   float* X = P.lev[0];
   const int64_t ld = P.ld[0];
@@ -201,10 +228,20 @@ __global__ void __launch_bounds__(256) tn_partial_kernel(int m, int rpc, int k1,
   for (int r0 = c * rpc; r0 < min(m, (c + 1) * rpc); r0 += CH) {
     const int mm = min(CH, m - r0);
     __syncthreads();
-    for (int e = threadIdx.x; e < CH * 64; e += 256) {
+    float xv[CH * 64 / 256], yv[CH * 64 / 256];
+#pragma unroll
+    for (int u = 0; u < CH * 64 / 256; ++u) {
+      const int e = threadIdx.x + 256 * u;
       const int r = e % CH, j = e / CH;
-      Xs[r][j] = (r < mm && j < k1) ? __ldcg(&X[r0 + r + static_cast<int64_t>(j) * ldx]) : 0.f;
-      Ys[r][j] = (r < mm && j < k2) ? __ldcg(&Y[r0 + r + static_cast<int64_t>(j) * ldy]) : 0.f;
+      const bool in = r < mm;
+      xv[u] = (in && j < k1) ? __ldcg(&X[r0 + r + static_cast<int64_t>(j) * ldx]) : 0.f;
+      yv[u] = (in && j < k2) ? __ldcg(&Y[r0 + r + static_cast<int64_t>(j) * ldy]) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < CH * 64 / 256; ++u) {
+      const int e = threadIdx.x + 256 * u;
+      Xs[e % CH][e / CH] = xv[u];
+      Ys[e % CH][e / CH] = yv[u];
     }
     __syncthreads();
 #pragma unroll 4
@@ -228,76 +265,120 @@ __global__ void __launch_bounds__(256) tn_partial_kernel(int m, int rpc, int k1,
     for (int v = 0; v < 4; ++v) out[(tx + 16 * u) + 64 * (ty + 16 * v)] = acc[u][v];
 }
 
-// R[i,j] (+)= sum over chunks in order (deterministic).
-__global__ void tn_reduce_kernel(int nch, int k1, int k2, const float* __restrict__ part, float* R, int64_t ldr,
-                                 int accumulate) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= 64 * 64) return;
-  const int i = e % 64, j = e / 64;
-  if (i >= k1 || j >= k2) return;
-  float s = 0.f;
-  for (int c = 0; c < nch; ++c) s += __ldcg(&part[static_cast<int64_t>(c) * 4096 + e]);
-  float* o = &R[i + static_cast<int64_t>(j) * ldr];
+// R[i,j] (+)= sum over chunks, deterministic: 32 outputs x 8 slices per block;
+// slice j sums chunks j, j+8, ... in order, slices combined in a fixed tree.
+__global__ void __launch_bounds__(256) tn_reduce_kernel(int nch, int k1, int k2, const float* __restrict__ part,
+                                                        float* R, int64_t ldr, int accumulate) {
+  __shared__ float sl[8][33];
+  const int e = blockIdx.x * 32 + threadIdx.x % 32;  // element of the 64x64 partial tile
+  const int j = threadIdx.x / 32;
+  float acc = 0.f;
+#pragma unroll 8
+  for (int c = j; c < nch; c += 8) acc += __ldcg(&part[static_cast<int64_t>(c) * 4096 + e]);
+  sl[j][threadIdx.x % 32] = acc;
+  __syncthreads();
+  if (j != 0) return;
+  const int l = threadIdx.x;
+  const float s = ((sl[0][l] + sl[1][l]) + (sl[2][l] + sl[3][l])) + ((sl[4][l] + sl[5][l]) + (sl[6][l] + sl[7][l]));
+  const int i = e % 64, jj = e / 64;
+  if (i >= k1 || jj >= k2) return;
+  float* o = &R[i + static_cast<int64_t>(jj) * ldr];
   *o = accumulate ? *o + s : s;
 }
 
-// Y[rows] -= X[rows] * S  with S (k1 x k2, k <= 64) from R (ldr).
+// Y[rows] -= X[rows] * S with S (k1 x k2, k <= 64) from R (lds). One CTA per
+// 64 rows: X and Y tiles staged in shared memory with all loads in flight,
+// each thread updates 4 rows x 4 columns.
+constexpr int NNR = 64;
 __global__ void __launch_bounds__(256) nn_update_kernel(int m, int k1, int k2, const float* __restrict__ X,
                                                         int64_t ldx, const float* __restrict__ S, int64_t lds,
-                                                        float* Y, int64_t ldy) {
+                                                        float* __restrict__ Y, int64_t ldy) {
   __shared__ float Ss[64][65];
-  for (int e = threadIdx.x; e < 64 * 64; e += 256) {
+  __shared__ float Xs[NNR][65];
+  const int r0 = blockIdx.x * NNR;
+  const int mm = min(NNR, m - r0);
+  float sv[16], xv[16];
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int e = threadIdx.x + 256 * u;
     const int i = e % 64, j = e / 64;
-    Ss[i][j] = (i < k1 && j < k2) ? S[i + static_cast<int64_t>(j) * lds] : 0.f;
+    sv[u] = (i < k1 && j < k2) ? S[i + static_cast<int64_t>(j) * lds] : 0.f;
+    xv[u] = (i < mm && j < k1) ? __ldcg(&X[r0 + i + static_cast<int64_t>(j) * ldx]) : 0.f;
+  }
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // rows tx + 16 a, cols ty + 16 b
+  float y[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = tx + 16 * u, j = ty + 16 * v;
+      y[u][v] = (i < mm && j < k2) ? __ldcg(&Y[r0 + i + static_cast<int64_t>(j) * ldy]) : 0.f;
+    }
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int e = threadIdx.x + 256 * u;
+    Ss[e % 64][e / 64] = sv[u];
+    Xs[e % 64][e / 64] = xv[u];
   }
   __syncthreads();
-  const int r = blockIdx.x * 128 + (threadIdx.x & 127);
-  const int half = threadIdx.x >> 7;  // columns [32 half, 32 half + 32)
-  if (r >= m) return;
-  float x[64];
+#pragma unroll 8
+  for (int k = 0; k < 64; ++k) {
+    float xr[4], sr[4];
 #pragma unroll
-  for (int k = 0; k < 64; ++k) x[k] = (k < k1) ? __ldcg(&X[r + static_cast<int64_t>(k) * ldx]) : 0.f;
-#pragma unroll 2
-  for (int jj = 0; jj < 32; ++jj) {
-    const int j = 32 * half + jj;
-    if (j >= k2) break;
-    float s = 0.f;
+    for (int u = 0; u < 4; ++u) {
+      xr[u] = Xs[tx + 16 * u][k];
+      sr[u] = Ss[k][ty + 16 * u];
+    }
 #pragma unroll
-    for (int k = 0; k < 64; ++k) s += x[k] * Ss[k][j];
-    float* y = &Y[r + static_cast<int64_t>(j) * ldy];
-    *y -= s;
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) y[u][v] -= xr[u] * sr[v];
   }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int i = tx + 16 * u, j = ty + 16 * v;
+      if (i < mm && j < k2) Y[r0 + i + static_cast<int64_t>(j) * ldy] = y[u][v];
+    }
 }
 
 }  // namespace
 
-// Level sizes of the TSQR tree for an m-row panel; returns the workspace need.
-void tsqr_plan_sizes(int m, int* nlev, int rows[kMaxTsqrLevels], int nblk[kMaxTsqrLevels], int64_t* stack_floats,
-                     int* ncounters) {
+// Level sizes of the TSQR tree for an m-row panel: 256-row blocks at every
+// level, eight 32x32 R factors stacked per block of the next level (the
+// reference's tree shape, QR/panel.cu:87-133). A 16384-row panel has three
+// levels (64, 8, 1 blocks).
+void tsqr_plan_sizes(int m, TsqrPlan* P, int64_t* stack_floats, int* ncounters) {
   int L = 0;
   int r = m;
   int64_t st = 0;
   int cnt = 0;
+  P->div[0] = 1;
   while (true) {
-    rows[L] = r;
-    nblk[L] = (r + BR - 1) / BR;
-    if (nblk[L] == 1 || L == kMaxTsqrLevels - 1) break;
-    cnt += (nblk[L] + 7) / 8;
-    r = 32 * nblk[L];
-    st += round_up(r, 64) * 32;
+    P->br[L] = BR;
+    P->rows[L] = r;
+    P->nblk[L] = (r + BR - 1) / BR;
+    if (P->nblk[L] == 1 || L == kMaxTsqrLevels - 1) break;
+    P->cnt_off[L] = cnt;
+    cnt += (P->nblk[L] + kGroup - 1) / kGroup;
+    r = PB * P->nblk[L];
+    P->div[L + 1] = P->div[L] * kGroup;
+    st += round_up(r, 64) * PB;
     ++L;
   }
-  *nlev = L + 1;
+  P->maxbr = BR;
+  P->nlev = L + 1;
   *stack_floats = st;
   *ncounters = cnt;
 }
 
 later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R, int64_t ldr, void* qh, void* ql,
-                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed) {
+                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed, long long budget) {
   TsqrPlan P{};
   int64_t stack = 0;
   int ncnt = 0;
-  tsqr_plan_sizes(m, &P.nlev, P.rows, P.nblk, &stack, &ncnt);
+  tsqr_plan_sizes(m, &P, &stack, &ncnt);
   if (P.nblk[P.nlev - 1] != 1 || ncnt > 2048) return LATER_ERR_NOT_SUPPORTED;  // m beyond the tree capacity
   P.lev[0] = A;
   P.ld[0] = lda;
@@ -307,22 +388,22 @@ later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R
     P.lev[L] = ws.take<float>(P.ld[L] * 32);
     if (!P.lev[L]) return LATER_ERR_WORKSPACE;
   }
-  int off = 0;
-  for (int L = 0; L < P.nlev - 1; ++L) {
-    P.cnt_off[L] = off;
-    off += (P.nblk[L] + 7) / 8;
-  }
   P.counters = counters_zeroed;
   P.R = R;
   P.ldr = ldr;
+  P.status = device_status_ptr();
+  P.budget = budget > 0 ? budget : kDefaultBudgetCycles;
   if (ws.sizing()) {
     ws.reset(mark);
     return LATER_OK;
   }
+  TraceScope trace(s, TRACE_PANEL);
   tsqr_reduce_kernel<<<P.nblk[0], 1024, 0, s>>>(P);
+  note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
   const int mode = out_prec == LATER_PREC_BF16 ? 1 : (out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
-  tsqr_apply_kernel<<<P.nblk[0], 256, 0, s>>>(P, qh, ql, ldh, mode);
+  tsqr_apply_kernel<<<(m + APPLY_ROWS - 1) / APPLY_ROWS, 256, 0, s>>>(P, qh, ql, ldh, mode);
+  note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
   ws.reset(mark);
   return LATER_OK;
@@ -331,8 +412,9 @@ later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R
 later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* Y,
                        int64_t ldy, float* R, int64_t ldr, int accumulate, Arena& ws) {
   // One partial 64x64 tile per CTA; as many CTAs (up to one per 128 rows) as
-  // the workspace holds partial tiles for.
+  // the workspace holds partial tiles for, at most 256.
   int nch = (m + 127) / 128;
+  if (nch > 256) nch = 256;
   const int64_t fit = static_cast<int64_t>(ws.remaining() / sizeof(float)) / 4096 - 1;
   if (!ws.sizing() && fit < nch) nch = fit < 1 ? 1 : static_cast<int>(fit);
   const int rpc = static_cast<int>(round_up((m + nch - 1) / nch, CH));
@@ -344,9 +426,12 @@ later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, in
     ws.reset(mark);
     return LATER_OK;
   }
+  TraceScope trace(s, TRACE_LEAF_GEMM, 2.0 * m * k1 * k2);
   tn_partial_kernel<<<nch, 256, 0, s>>>(m, rpc, k1, k2, X, ldx, Y, ldy, part);
+  note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
-  tn_reduce_kernel<<<16, 256, 0, s>>>(nch, k1, k2, part, R, ldr, accumulate);
+  tn_reduce_kernel<<<4096 / 32, 256, 0, s>>>(nch, k1, k2, part, R, ldr, accumulate);
+  note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
   ws.reset(mark);
   return LATER_OK;
@@ -354,7 +439,9 @@ later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, in
 
 later_status_t simt_nn_sub(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* S,
                            int64_t lds, float* Y, int64_t ldy) {
-  nn_update_kernel<<<(m + 127) / 128, 256, 0, s>>>(m, k1, k2, X, ldx, S, lds, Y, ldy);
+  TraceScope trace(s, TRACE_LEAF_GEMM, 2.0 * m * k1 * k2);
+  nn_update_kernel<<<(m + NNR - 1) / NNR, 256, 0, s>>>(m, k1, k2, X, ldx, S, lds, Y, ldy);
+  note_launch();
   return cuda_status(cudaGetLastError());
 }
 

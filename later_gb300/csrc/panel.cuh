@@ -12,6 +12,9 @@ constexpr int kMaxTsqrLevels = 8;
 // L >= 1 is the stack of the 32x32 R factors of level L-1 (32 rows per block).
 struct TsqrPlan {
   int nlev;
+  int maxbr;                      // tallest block of any level
+  int br[kMaxTsqrLevels];         // rows per block at level L (256, 512 or 1024)
+  int div[kMaxTsqrLevels];        // level-0 blocks per level-L block
   float* lev[kMaxTsqrLevels];
   int64_t ld[kMaxTsqrLevels];
   int rows[kMaxTsqrLevels];
@@ -20,15 +23,16 @@ struct TsqrPlan {
   int* counters;
   float* R;
   int64_t ldr;
+  int* status;
+  long long budget;
 };
 
-void tsqr_plan_sizes(int m, int* nlev, int rows[kMaxTsqrLevels], int nblk[kMaxTsqrLevels], int64_t* stack_floats,
-                     int* ncounters);
+void tsqr_plan_sizes(int m, TsqrPlan* P, int64_t* stack_floats, int* ncounters);
 
 // QR of the m x 32 panel A: Q overwrites A (FP32) and is also written to the
 // 16-bit copy (qh / ql, may be null); R (32x32, upper) goes to R.
 later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R, int64_t ldr, void* qh, void* ql,
-                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed);
+                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed, long long budget);
 
 // R (+)= X^T Y for X (m x k1), Y (m x k2), k1, k2 <= 64, FP32.
 later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* Y,

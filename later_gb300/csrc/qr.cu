@@ -70,7 +70,7 @@ Scratch gemm_scratch(Ctx& c) {
 later_status_t leaf_qr(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
   if (w <= 32) {
     return tsqr_panel(c.st, c.m, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
-                      c.o.prec, *c.ws, c.counters);
+                      c.o.prec, *c.ws, c.counters, c.o.budget);
   }
   const int w1 = split_half(w), w2 = w - w1;
   LATER_CHECK(leaf_qr(c, w1, A, lda, R, ldr, col));
@@ -184,9 +184,10 @@ QrNeed rgsqrf_need(int m, int n, const Options& o) {
   Layout L;
   carve(a, n, o, &L);
   const int64_t fixed = static_cast<int64_t>(a.peak() / sizeof(float)) + 64;
-  int nlev, rows[kMaxTsqrLevels], nblk[kMaxTsqrLevels], ncnt;
+  TsqrPlan plan{};
+  int ncnt;
   int64_t stack;
-  tsqr_plan_sizes(m, &nlev, rows, nblk, &stack, &ncnt);
+  tsqr_plan_sizes(m, &plan, &stack, &ncnt);
   stack += 64 * kMaxTsqrLevels;
   const int64_t leaf_parts = ((m + 127) / 128) * 4096 + 128;
   const int64_t splitk = static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 128;

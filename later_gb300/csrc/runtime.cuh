@@ -102,6 +102,26 @@ later_status_t axpy2d(cudaStream_t st, int m, int n, float alpha, const float* X
 // Y = X (m x n blocks).
 later_status_t copy2d(cudaStream_t st, int m, int n, const float* X, int64_t ldx, float* Y, int64_t ldy);
 
+// ------------------------------------------------------------- tracing
+enum TraceKind { TRACE_GEMM = 0, TRACE_PANEL = 1, TRACE_LEAF_GEMM = 2, TRACE_OTHER = 3 };
+void note_launch(int n = 1);
+// Brackets the launches issued during its lifetime with CUDA events on `st`
+// while tracing is on (later_c_trace_begin); otherwise does nothing.
+class TraceScope {
+ public:
+  TraceScope(cudaStream_t st, int kind, double flops = 0.0);
+  ~TraceScope();
+  TraceScope(const TraceScope&) = delete;
+  TraceScope& operator=(const TraceScope&) = delete;
+
+ private:
+  cudaStream_t st_;
+  int kind_;
+  double flops_;
+  bool on_ = false;
+  cudaEvent_t a_{}, b_{};
+};
+
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 
 }  // namespace later

@@ -125,20 +125,26 @@ inline dim3 grid2d(int m, int n) {
 
 later_status_t fill_strict_lower(cudaStream_t st, int m, int n, float* A, int64_t lda, float v) {
   if (m <= 0 || n <= 0) return LATER_OK;
+  TraceScope trace(st, TRACE_OTHER);
   fill_strict_lower_kernel<<<grid2d(m, n), 256, 0, st>>>(m, n, A, lda, v);
+  note_launch();
   return cuda_status(cudaGetLastError());
 }
 
 later_status_t axpy2d(cudaStream_t st, int m, int n, float alpha, const float* X, int64_t ldx, float* Y,
                       int64_t ldy) {
   if (m <= 0 || n <= 0) return LATER_OK;
+  TraceScope trace(st, TRACE_OTHER);
   axpy2d_kernel<<<grid2d(m, n), 256, 0, st>>>(m, n, alpha, X, ldx, Y, ldy);
+  note_launch();
   return cuda_status(cudaGetLastError());
 }
 
 later_status_t copy2d(cudaStream_t st, int m, int n, const float* X, int64_t ldx, float* Y, int64_t ldy) {
   if (m <= 0 || n <= 0) return LATER_OK;
+  TraceScope trace(st, TRACE_OTHER);
   copy2d_kernel<<<grid2d(m, n), 256, 0, st>>>(m, n, X, ldx, Y, ldy);
+  note_launch();
   return cuda_status(cudaGetLastError());
 }
 
@@ -158,7 +164,9 @@ later_status_t convert16(cudaStream_t st, int m, int n, const float* A, int64_t 
     }
     return LATER_OK;
   }
+  TraceScope trace(st, TRACE_OTHER);
   convert_kernel<<<grid, block, 0, st>>>(m, n, A, lda, hi, lo, ldh, prec, device_status_ptr());
+  note_launch();
   return cuda_status(cudaGetLastError());
 }
 
