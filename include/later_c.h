@@ -75,6 +75,35 @@ later_status_t later_c_rgsqrf(later_stream_t stream, int m, int n, float* A, int
                               float* work, int64_t lwork, void* hwork, int64_t lhwork,
                               const later_options_t* opt);
 
+/* Minimum `work` (floats) and `hwork` (16-bit elements) for later_c_rhouqr. */
+later_status_t later_c_rhouqr_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork,
+                                      int64_t* lhwork);
+
+/*
+ * Recursive Householder QR in compact-WY form: Q = I - W Y^T, A = Q R.
+ * Replaces LATER include/LATER.h:41 later_rhouqr (QR/later_rhouqr.cu:27-201).
+ * A (m x n) is overwritten by Y (unit lower trapezoidal Householder vectors,
+ * LAPACK dgeqrf's V); W (m x n) receives W = Y T; R (n x n) the upper factor
+ * with LAPACK's sign convention and zeros below the diagonal.
+ * Requires m >= n and n a multiple of 32. (The reference's 32x32 `U` scratch
+ * argument is not needed: the reconstruction scratch lives in `work`.)
+ */
+later_status_t later_c_rhouqr(later_stream_t stream, int m, int n, float* A, int lda, float* W, int ldw,
+                              float* R, int ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                              const later_options_t* opt);
+
+/*
+ * Explicit Q = I - W Y^T (first n columns), written over W, in FP32.
+ * Replaces LATER include/LATER.h:43 later_ormqr and :47 later_ormqr2
+ * (QR/later_ormqr.cu:18-86). `work` holds m*n floats. Unlike the reference's
+ * later_ormqr, W is used as rhouqr returns it (already merged): the
+ * reference repeats the top-level W merge (QR/later_ormqr.cu:27-45) that its
+ * rhouqr already performed (QR/later_rhouqr.cu:150-199, the `n < ori_n`
+ * guard is commented out), which would apply Q1 twice.
+ */
+later_status_t later_c_ormqr(later_stream_t stream, int m, int n, float* W, int ldw, const float* Y, int ldy,
+                             float* work, int64_t lwork);
+
 /* --------------------------------------------------------- building blocks */
 
 /*

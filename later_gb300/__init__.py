@@ -19,7 +19,7 @@ from . import build as _build
 
 __all__ = [
     "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
-    "later_rgsqrf", "rgsqrf_bufsize", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
+    "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
     "trace_end",
 ]
 
@@ -56,6 +56,9 @@ _SIGS = {
     "later_c_gemm16": (_i, [_vp, ctypes.c_char, ctypes.c_char, _i, _i, _i, _f, _vp, _i, _vp, _i, _f, _vp, _i,
                             _vp, _i, _i, _vp, _i64]),
     "later_c_convert": (_i, [_vp, _i, _i, _vp, _i, _vp, _vp, _i, _i]),
+    "later_c_rhouqr_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "later_c_rhouqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
+    "later_c_ormqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i64]),
     "later_c_launch_count": (ctypes.c_uint64, []),
     "later_c_trace_begin": (None, []),
     "later_c_trace_end": (_i, [_vp]),
@@ -175,6 +178,48 @@ def later_rgsqrf(A, R=None, work=None, hwork=None, *, precision="fp16", cgs2=Fal
     _check(lib().later_c_rgsqrf(_stream(stream), m, n, A.data_ptr(), lda, R.data_ptr(), ldr, work.data_ptr(),
                                 work.numel(), hwork.data_ptr(), hwork.numel(), ctypes.byref(o)), "later_rgsqrf")
     return R
+
+
+def rhouqr_bufsize(m, n, precision="fp16"):
+    o = Options.make(precision)
+    lw, lh = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().later_c_rhouqr_bufsize(m, n, ctypes.byref(o), ctypes.byref(lw), ctypes.byref(lh)), "rhouqr_bufsize")
+    return lw.value, lh.value
+
+
+def later_rhouqr(A, W=None, R=None, work=None, hwork=None, *, precision="fp16", timeout_cycles=0, stream=None):
+    """Recursive Householder QR: A becomes Y; returns (W, R) with Q = I - W Y^T.
+
+    Mirrors LATER's `later_rhouqr(ctxt, m, n, A, lda, W, ldw, R, ldr, work, lwork, hwork, lhwork, U)`
+    (include/LATER.h:41).
+    """
+    import torch
+    m, n = A.shape
+    if W is None:
+        W = empty_colmajor(m, n, device=A.device)
+    if R is None:
+        R = empty_colmajor(n, n, device=A.device)
+    lw, lh = rhouqr_bufsize(m, n, precision)
+    if work is None:
+        work = torch.empty(lw, dtype=torch.float32, device=A.device)
+    if hwork is None:
+        hwork = torch.empty(lh, dtype=torch.float16, device=A.device)
+    o = Options.make(precision, False, 128, timeout_cycles)
+    _check(lib().later_c_rhouqr(_stream(stream), m, n, A.data_ptr(), _ld(A, "A"), W.data_ptr(), _ld(W, "W"),
+                                R.data_ptr(), _ld(R, "R"), work.data_ptr(), work.numel(), hwork.data_ptr(),
+                                hwork.numel(), ctypes.byref(o)), "later_rhouqr")
+    return W, R
+
+
+def later_ormqr(W, Y, work=None, stream=None):
+    """Explicit Q = I - W Y^T (first n columns) written over W (include/LATER.h:43)."""
+    import torch
+    m, n = W.shape
+    if work is None:
+        work = torch.empty(m * n, dtype=torch.float32, device=W.device)
+    _check(lib().later_c_ormqr(_stream(stream), m, n, W.data_ptr(), _ld(W, "W"), Y.data_ptr(), _ld(Y, "Y"),
+                               work.data_ptr(), work.numel()), "later_ormqr")
+    return W
 
 
 def gemm16(transa, transb, A, B, alpha=1.0, beta=0.0, C=None, D=None, precision="fp16", work=None, stream=None):

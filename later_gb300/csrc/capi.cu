@@ -61,6 +61,26 @@ later_status_t later_c_rgsqrf(later_stream_t stream, int m, int n, float* A, int
                 options_from(opt));
 }
 
+later_status_t later_c_rhouqr_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork, int64_t* lhwork) {
+  if (m < 1 || n < 1 || m < n) return LATER_ERR_INVALID_ARG;
+  const QrNeed q = rhouqr_need(m, n, options_from(opt));
+  if (lwork) *lwork = q.rec_work;
+  if (lhwork) *lhwork = q.hwork;
+  return LATER_OK;
+}
+
+later_status_t later_c_rhouqr(later_stream_t stream, int m, int n, float* A, int lda, float* W, int ldw, float* R,
+                              int ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                              const later_options_t* opt) {
+  return rhouqr(reinterpret_cast<cudaStream_t>(stream), m, n, A, lda, W, ldw, R, ldr, work, lwork, hwork, lhwork,
+                options_from(opt));
+}
+
+later_status_t later_c_ormqr(later_stream_t stream, int m, int n, float* W, int ldw, const float* Y, int ldy,
+                             float* work, int64_t lwork) {
+  return ormqr(reinterpret_cast<cudaStream_t>(stream), m, n, W, ldw, Y, ldy, work, lwork);
+}
+
 later_status_t later_c_gemm16(later_stream_t stream, char transa, char transb, int m, int n, int k, float alpha,
                               const void* A, int lda, const void* B, int ldb, float beta, const float* C, int ldc,
                               float* D, int ldd, int precision, float* work, int64_t lwork) {

@@ -15,6 +15,8 @@
 // (tsqr_apply_kernel) composes each block's path through the tree (32x32
 // products) and writes the final Q in FP32 together with its 16-bit copy, so
 // the tensor-core GEMMs that follow need no conversion pass.
+#include <algorithm>
+
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -215,7 +217,8 @@ __global__ void __launch_bounds__(256) tsqr_apply_kernel(TsqrPlan P, void* qh, v
 }
 
 // ---------------------------------------------------------- FP32 SIMT GEMMs
-// Partial products P[c] = X[rows of chunk c]^T Y[rows of chunk c] for k1, k2 <= 64.
+// Partial products P[c][t] = X[rows of chunk c]^T Y[rows of chunk c] for the
+// 64x64 output tile t = (ti, tj): grid (chunks, tiles_i * tiles_j).
 constexpr int CH = 64;  // rows per shared-memory tile; a CTA covers `rpc` rows (multiple of CH)
 __global__ void __launch_bounds__(256) tn_partial_kernel(int m, int rpc, int k1, int k2, const float* __restrict__ X,
                                                          int64_t ldx, const float* __restrict__ Y, int64_t ldy,
@@ -223,6 +226,9 @@ __global__ void __launch_bounds__(256) tn_partial_kernel(int m, int rpc, int k1,
   __shared__ float Xs[CH][65];
   __shared__ float Ys[CH][65];
   const int c = blockIdx.x;
+  const int ti_n = (k1 + 63) / 64;
+  const int ti = blockIdx.y % ti_n, tj = blockIdx.y / ti_n;
+  const int i0 = ti * 64, j0 = tj * 64;
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   float acc[4][4] = {};
   for (int r0 = c * rpc; r0 < min(m, (c + 1) * rpc); r0 += CH) {
@@ -234,8 +240,8 @@ __global__ void __launch_bounds__(256) tn_partial_kernel(int m, int rpc, int k1,
       const int e = threadIdx.x + 256 * u;
       const int r = e % CH, j = e / CH;
       const bool in = r < mm;
-      xv[u] = (in && j < k1) ? __ldcg(&X[r0 + r + static_cast<int64_t>(j) * ldx]) : 0.f;
-      yv[u] = (in && j < k2) ? __ldcg(&Y[r0 + r + static_cast<int64_t>(j) * ldy]) : 0.f;
+      xv[u] = (in && i0 + j < k1) ? __ldcg(&X[r0 + r + static_cast<int64_t>(i0 + j) * ldx]) : 0.f;
+      yv[u] = (in && j0 + j < k2) ? __ldcg(&Y[r0 + r + static_cast<int64_t>(j0 + j) * ldy]) : 0.f;
     }
 #pragma unroll
     for (int u = 0; u < CH * 64 / 256; ++u) {
@@ -258,7 +264,7 @@ __global__ void __launch_bounds__(256) tn_partial_kernel(int m, int rpc, int k1,
         for (int v = 0; v < 4; ++v) acc[u][v] += x[u] * y[v];
     }
   }
-  float* out = part + static_cast<int64_t>(c) * 64 * 64;
+  float* out = part + (static_cast<int64_t>(c) * gridDim.y + blockIdx.y) * 4096;
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -267,79 +273,101 @@ __global__ void __launch_bounds__(256) tn_partial_kernel(int m, int rpc, int k1,
 
 // R[i,j] (+)= sum over chunks, deterministic: 32 outputs x 8 slices per block;
 // slice j sums chunks j, j+8, ... in order, slices combined in a fixed tree.
-__global__ void __launch_bounds__(256) tn_reduce_kernel(int nch, int k1, int k2, const float* __restrict__ part,
-                                                        float* R, int64_t ldr, int accumulate) {
+__global__ void __launch_bounds__(256) tn_reduce_kernel(int nch, int ntiles, int k1, int k2,
+                                                        const float* __restrict__ part, float* R, int64_t ldr,
+                                                        int accumulate) {
   __shared__ float sl[8][33];
-  const int e = blockIdx.x * 32 + threadIdx.x % 32;  // element of the 64x64 partial tile
+  const int t = blockIdx.x / 128;                     // output tile
+  const int e = (blockIdx.x % 128) * 32 + threadIdx.x % 32;  // element of the 64x64 tile
   const int j = threadIdx.x / 32;
   float acc = 0.f;
 #pragma unroll 8
-  for (int c = j; c < nch; c += 8) acc += __ldcg(&part[static_cast<int64_t>(c) * 4096 + e]);
+  for (int c = j; c < nch; c += 8) acc += __ldcg(&part[(static_cast<int64_t>(c) * ntiles + t) * 4096 + e]);
   sl[j][threadIdx.x % 32] = acc;
   __syncthreads();
   if (j != 0) return;
   const int l = threadIdx.x;
   const float s = ((sl[0][l] + sl[1][l]) + (sl[2][l] + sl[3][l])) + ((sl[4][l] + sl[5][l]) + (sl[6][l] + sl[7][l]));
-  const int i = e % 64, jj = e / 64;
+  const int ti_n = (k1 + 63) / 64;
+  const int i = (t % ti_n) * 64 + e % 64, jj = (t / ti_n) * 64 + e / 64;
   if (i >= k1 || jj >= k2) return;
   float* o = &R[i + static_cast<int64_t>(jj) * ldr];
   *o = accumulate ? *o + s : s;
 }
 
-// Y[rows] -= X[rows] * S with S (k1 x k2, k <= 64) from R (lds). One CTA per
-// 64 rows: X and Y tiles staged in shared memory with all loads in flight,
-// each thread updates 4 rows x 4 columns.
+// Y[rows, cols] -= X[rows, :] * S[:, cols] with S (k1 x k2). One CTA per 64
+// rows x 64 columns; the inner dimension is walked in chunks of 64 with X and
+// S staged in shared memory; each thread updates 4 rows x 4 columns. Optional
+// 16-bit copy of the updated Y (mode 0 fp16, 1 bf16, 2 split3 hi/lo).
 constexpr int NNR = 64;
 __global__ void __launch_bounds__(256) nn_update_kernel(int m, int k1, int k2, const float* __restrict__ X,
                                                         int64_t ldx, const float* __restrict__ S, int64_t lds,
-                                                        float* __restrict__ Y, int64_t ldy) {
+                                                        float* __restrict__ Y, int64_t ldy, void* yh, void* yl,
+                                                        int64_t ldh, int mode) {
   __shared__ float Ss[64][65];
   __shared__ float Xs[NNR][65];
   const int r0 = blockIdx.x * NNR;
+  const int c0 = blockIdx.y * 64;
   const int mm = min(NNR, m - r0);
-  float sv[16], xv[16];
-#pragma unroll
-  for (int u = 0; u < 16; ++u) {
-    const int e = threadIdx.x + 256 * u;
-    const int i = e % 64, j = e / 64;
-    sv[u] = (i < k1 && j < k2) ? S[i + static_cast<int64_t>(j) * lds] : 0.f;
-    xv[u] = (i < mm && j < k1) ? __ldcg(&X[r0 + i + static_cast<int64_t>(j) * ldx]) : 0.f;
-  }
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // rows tx + 16 a, cols ty + 16 b
   float y[4][4];
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const int i = tx + 16 * u, j = ty + 16 * v;
+      const int i = tx + 16 * u, j = c0 + ty + 16 * v;
       y[u][v] = (i < mm && j < k2) ? __ldcg(&Y[r0 + i + static_cast<int64_t>(j) * ldy]) : 0.f;
     }
+  for (int k0 = 0; k0 < k1; k0 += 64) {
+    float sv[16], xv[16];
 #pragma unroll
-  for (int u = 0; u < 16; ++u) {
-    const int e = threadIdx.x + 256 * u;
-    Ss[e % 64][e / 64] = sv[u];
-    Xs[e % 64][e / 64] = xv[u];
-  }
-  __syncthreads();
-#pragma unroll 8
-  for (int k = 0; k < 64; ++k) {
-    float xr[4], sr[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      xr[u] = Xs[tx + 16 * u][k];
-      sr[u] = Ss[k][ty + 16 * u];
+    for (int u = 0; u < 16; ++u) {
+      const int e = threadIdx.x + 256 * u;
+      const int i = e % 64, j = e / 64;
+      sv[u] = (k0 + i < k1 && c0 + j < k2) ? S[k0 + i + static_cast<int64_t>(c0 + j) * lds] : 0.f;
+      xv[u] = (i < mm && k0 + j < k1) ? __ldcg(&X[r0 + i + static_cast<int64_t>(k0 + j) * ldx]) : 0.f;
     }
+    __syncthreads();
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 16; ++u) {
+      const int e = threadIdx.x + 256 * u;
+      Ss[e % 64][e / 64] = sv[u];
+      Xs[e % 64][e / 64] = xv[u];
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < 64; ++k) {
+      float xr[4], sr[4];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) y[u][v] -= xr[u] * sr[v];
+      for (int u = 0; u < 4; ++u) {
+        xr[u] = Xs[tx + 16 * u][k];
+        sr[u] = Ss[k][ty + 16 * u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) y[u][v] -= xr[u] * sr[v];
+    }
   }
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const int i = tx + 16 * u, j = ty + 16 * v;
-      if (i < mm && j < k2) Y[r0 + i + static_cast<int64_t>(j) * ldy] = y[u][v];
+      const int i = tx + 16 * u, j = c0 + ty + 16 * v;
+      if (i < mm && j < k2) {
+        const float val = y[u][v];
+        Y[r0 + i + static_cast<int64_t>(j) * ldy] = val;
+        if (yh) {
+          const int64_t o = r0 + i + static_cast<int64_t>(j) * ldh;
+          if (mode == 1) {
+            reinterpret_cast<__nv_bfloat16*>(yh)[o] = __float2bfloat16_rn(val);
+          } else {
+            const __half h = __float2half_rn(val);
+            reinterpret_cast<__half*>(yh)[o] = h;
+            if (mode == 2) reinterpret_cast<__half*>(yl)[o] = __float2half_rn((val - __half2float(h)) * 2048.f);
+          }
+        }
+      }
     }
 }
 
@@ -411,26 +439,29 @@ later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R
 
 later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* Y,
                        int64_t ldy, float* R, int64_t ldr, int accumulate, Arena& ws) {
-  // One partial 64x64 tile per CTA; as many CTAs (up to one per 128 rows) as
-  // the workspace holds partial tiles for, at most 256.
+  if (m <= 0 || k1 <= 0 || k2 <= 0) return LATER_OK;
+  // Partial 64x64 tiles per (row chunk, output tile); as many row chunks (up
+  // to one per 128 rows, at most 256) as the workspace holds.
+  const int ntiles = ((k1 + 63) / 64) * ((k2 + 63) / 64);
   int nch = (m + 127) / 128;
   if (nch > 256) nch = 256;
-  const int64_t fit = static_cast<int64_t>(ws.remaining() / sizeof(float)) / 4096 - 1;
+  if (nch * ntiles > 4096) nch = std::max(1, 4096 / ntiles);
+  const int64_t fit = static_cast<int64_t>(ws.remaining() / sizeof(float)) / (4096LL * ntiles) - 1;
   if (!ws.sizing() && fit < nch) nch = fit < 1 ? 1 : static_cast<int>(fit);
   const int rpc = static_cast<int>(round_up((m + nch - 1) / nch, CH));
   nch = (m + rpc - 1) / rpc;
   const size_t mark = ws.used();
-  float* part = ws.take<float>(static_cast<size_t>(nch) * 4096);
+  float* part = ws.take<float>(static_cast<size_t>(nch) * ntiles * 4096);
   if (!part) return LATER_ERR_WORKSPACE;
   if (ws.sizing()) {
     ws.reset(mark);
     return LATER_OK;
   }
   TraceScope trace(s, TRACE_LEAF_GEMM, 2.0 * m * k1 * k2);
-  tn_partial_kernel<<<nch, 256, 0, s>>>(m, rpc, k1, k2, X, ldx, Y, ldy, part);
+  tn_partial_kernel<<<dim3(nch, ntiles), 256, 0, s>>>(m, rpc, k1, k2, X, ldx, Y, ldy, part);
   note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
-  tn_reduce_kernel<<<4096 / 32, 256, 0, s>>>(nch, k1, k2, part, R, ldr, accumulate);
+  tn_reduce_kernel<<<ntiles * 128, 256, 0, s>>>(nch, ntiles, k1, k2, part, R, ldr, accumulate);
   note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
   ws.reset(mark);
@@ -438,9 +469,13 @@ later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, in
 }
 
 later_status_t simt_nn_sub(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* S,
-                           int64_t lds, float* Y, int64_t ldy) {
+                           int64_t lds, float* Y, int64_t ldy, void* yh, void* yl, int64_t ldh, int out_prec) {
+  if (m <= 0 || k1 <= 0 || k2 <= 0) return LATER_OK;
+  if ((k2 + 63) / 64 > 65535) return LATER_ERR_NOT_SUPPORTED;
+  const int mode = out_prec == LATER_PREC_BF16 ? 1 : (out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
   TraceScope trace(s, TRACE_LEAF_GEMM, 2.0 * m * k1 * k2);
-  nn_update_kernel<<<(m + NNR - 1) / NNR, 256, 0, s>>>(m, k1, k2, X, ldx, S, lds, Y, ldy);
+  nn_update_kernel<<<dim3((m + NNR - 1) / NNR, (k2 + 63) / 64), 256, 0, s>>>(m, k1, k2, X, ldx, S, lds, Y, ldy, yh,
+                                                                             yl, ldh, mode);
   note_launch();
   return cuda_status(cudaGetLastError());
 }

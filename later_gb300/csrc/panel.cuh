@@ -34,12 +34,14 @@ void tsqr_plan_sizes(int m, TsqrPlan* P, int64_t* stack_floats, int* ncounters);
 later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R, int64_t ldr, void* qh, void* ql,
                           int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed, long long budget);
 
-// R (+)= X^T Y for X (m x k1), Y (m x k2), k1, k2 <= 64, FP32.
+// R (+)= X^T Y for X (m x k1), Y (m x k2), FP32 (SIMT, deterministic split over rows).
 later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* Y,
                        int64_t ldy, float* R, int64_t ldr, int accumulate, Arena& ws);
 
-// Y -= X S for X (m x k1), S (k1 x k2), k1, k2 <= 64, FP32.
+// Y -= X S for X (m x k1), S (k1 x k2), FP32 (SIMT); optional 16-bit copy of
+// the updated Y (yh / yl with leading dimension ldh, format out_prec).
 later_status_t simt_nn_sub(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* S,
-                           int64_t lds, float* Y, int64_t ldy);
+                           int64_t lds, float* Y, int64_t ldy, void* yh = nullptr, void* yl = nullptr,
+                           int64_t ldh = 0, int out_prec = LATER_PREC_FP16);
 
 }  // namespace later

@@ -15,6 +15,7 @@
 
 #include <algorithm>
 
+#include "householder.cuh"
 #include "panel.cuh"
 #include "qr.cuh"
 
@@ -231,6 +232,218 @@ later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, floa
   LATER_CHECK(convert16(st, m, n - f, A + static_cast<int64_t>(f) * lda, lda, c.sh_hi + f * c.ldh * 2,
                         c.sh_lo ? c.sh_lo + f * c.ldh * 2 : nullptr, c.ldh, o.prec));
   return rec_qr(c, n, A, lda, R, ldr, 0);
+}
+
+// ======================================================================
+// Recursive Householder QR (QR/later_rhouqr.cu:27-201):
+//   leaf (n <= 32): TSQR -> explicit Q -> Householder reconstruction (Y, W)
+//   else: qr(left); A2 <- (I - Y1 W1^T) A2; qr(bottom-right); R12 <- A2 top,
+//         zero it; W2 <- W2 - W1 (Y1^T W2)   (compact-WY merge)
+// GEMMs run on the tensor cores (precision option) when n/2 > 128 and
+// m > 128, else in FP32 SIMT kernels — the reference's own split (:83 Sgemm
+// vs GemmEx). The top n/2 rows of each merged W2 are zeroed explicitly (the
+// reference leaves them as they were in the caller's W).
+namespace {
+
+struct HCtx {
+  cudaStream_t st;
+  Options o;
+  Arena* ws;
+  int* counters;
+  int64_t ldh;
+  char* ah;  // 16-bit copy of A (then Y), hi / lo
+  char* al;
+  char* wh;  // 16-bit copy of W
+  char* wl;
+  float* work32;  // n1 x n2 FP32 product (top-level size)
+  void* workh;    // its 16-bit copy
+  void* workl;
+  int64_t ldwk;
+  HrScratch hr;
+};
+
+inline char* at16(char* base, int64_t ld, int64_t r, int64_t c) { return base ? base + (r + c * ld) * 2 : nullptr; }
+
+// C (k1 x k2) = X^T Z over mr rows, then Z' = Z - V C, through the tensor
+// cores (16-bit copies xh/zh/vh) or FP32 SIMT.
+later_status_t apply_block(HCtx& c, bool tc, int mr, int k1, int k2, const float* X, int64_t ldx, const char* xh,
+                           const char* xl, float* Z, int64_t ldz, char* zh, char* zl, const float* V, int64_t ldv,
+                           const char* vh, const char* vl) {
+  if (!tc) {
+    LATER_CHECK(simt_tn(c.st, mr, k1, k2, X, ldx, Z, ldz, c.work32, c.ldwk, 0, *c.ws));
+    return simt_nn_sub(c.st, mr, k1, k2, V, ldv, c.work32, c.ldwk, Z, ldz, zh, zl, c.ldh, c.o.prec);
+  }
+  Scratch sc;
+  sc.counters = c.counters + 2048;
+  sc.n_counters = 2048;
+  const int64_t avail = static_cast<int64_t>(c.ws->remaining() / sizeof(float)) - 64;
+  sc.partial_floats = std::max<int64_t>(0, std::min<int64_t>(avail, static_cast<int64_t>(num_sms()) * 128 * 256 * 2));
+  sc.partial = sc.partial_floats > 0 ? reinterpret_cast<float*>(
+                                           (reinterpret_cast<uintptr_t>(c.ws->cursor()) + 255) & ~uintptr_t(255))
+                                     : nullptr;
+  if (sc.partial_floats > 0) sc.partial_floats -= 64;
+  GemmCall tn;
+  tn.ta = 'T';
+  tn.tb = 'N';
+  tn.M = k1;
+  tn.N = k2;
+  tn.K = mr;
+  tn.A = Op16{xh, xl, c.ldh};
+  tn.B = Op16{zh, zl, c.ldh};
+  tn.out.D = c.work32;
+  tn.out.ldd = c.ldwk;
+  tn.out.Dh = c.workh;
+  tn.out.Dl = c.workl;
+  tn.out.ldh = c.ldwk;
+  tn.prec = c.o.prec;
+  tn.out_prec = c.o.prec;
+  LATER_CHECK(tc_gemm(tn, sc, c.st, c.o.budget));
+  GemmCall nn;
+  nn.ta = 'N';
+  nn.tb = 'N';
+  nn.M = mr;
+  nn.N = k2;
+  nn.K = k1;
+  nn.A = Op16{vh, vl, c.ldh};
+  nn.B = Op16{c.workh, c.workl, c.ldwk};
+  nn.alpha = -1.f;
+  nn.beta = 1.f;
+  nn.out.C = Z;
+  nn.out.ldc = ldz;
+  nn.out.D = Z;
+  nn.out.ldd = ldz;
+  nn.out.Dh = zh;
+  nn.out.Dl = zl;
+  nn.out.ldh = c.ldh;
+  nn.prec = c.o.prec;
+  nn.out_prec = c.o.prec;
+  return tc_gemm(nn, sc, c.st, c.o.budget);
+}
+
+// Sub-problem rows [r0, r0 + mr), columns [c0, c0 + n).
+later_status_t rec_hou(HCtx& c, int r0, int mr, int c0, int n, float* A0, int64_t lda, float* W0, int64_t ldw,
+                       float* R0, int64_t ldr) {
+  float* A = A0 + r0 + c0 * lda;
+  float* W = W0 + r0 + c0 * ldw;
+  float* R = R0 + c0 + c0 * ldr;
+  if (n <= 32) {
+    LATER_CHECK(tsqr_panel(c.st, mr, A, lda, R, ldr, nullptr, nullptr, 0, c.o.prec, *c.ws, c.counters, c.o.budget));
+    return householder_reconstruct(c.st, mr, n, A, lda, W, ldw, R, ldr, at16(c.ah, c.ldh, r0, c0),
+                                   at16(c.al, c.ldh, r0, c0), at16(c.wh, c.ldh, r0, c0), at16(c.wl, c.ldh, r0, c0),
+                                   c.ldh, c.o.prec, c.hr);
+  }
+  const int n1 = split_half(n), n2 = n - n1;
+  LATER_CHECK(rec_hou(c, r0, mr, c0, n1, A0, lda, W0, ldw, R0, ldr));
+  const bool tc = (n1 > 128 && mr > 128);
+  // A2 <- (I - Y1 W1^T) A2 : work = W1^T A2, A2 -= Y1 work
+  LATER_CHECK(apply_block(c, tc, mr, n1, n2, W, ldw, at16(c.wh, c.ldh, r0, c0), at16(c.wl, c.ldh, r0, c0),
+                          A + n1 * lda, lda, at16(c.ah, c.ldh, r0, c0 + n1), at16(c.al, c.ldh, r0, c0 + n1), A, lda,
+                          at16(c.ah, c.ldh, r0, c0), at16(c.al, c.ldh, r0, c0)));
+  LATER_CHECK(rec_hou(c, r0 + n1, mr - n1, c0 + n1, n2, A0, lda, W0, ldw, R0, ldr));
+  // R12 <- top of A2; zero it (and the top of W2) so that Y2 / W2 are full-height.
+  LATER_CHECK(copy2d(c.st, n1, n2, A + n1 * lda, lda, R + n1 * ldr, ldr));
+  LATER_CHECK(zero_block(c.st, n1, n2, A + n1 * lda, lda, at16(c.ah, c.ldh, r0, c0 + n1),
+                         at16(c.al, c.ldh, r0, c0 + n1), c.ldh));
+  LATER_CHECK(zero_block(c.st, n1, n2, W + n1 * ldw, ldw, at16(c.wh, c.ldh, r0, c0 + n1),
+                         at16(c.wl, c.ldh, r0, c0 + n1), c.ldh));
+  // W2 <- W2 - W1 (Y1^T W2)
+  return apply_block(c, tc, mr, n1, n2, A, lda, at16(c.ah, c.ldh, r0, c0), at16(c.al, c.ldh, r0, c0), W + n1 * ldw,
+                     ldw, at16(c.wh, c.ldh, r0, c0 + n1), at16(c.wl, c.ldh, r0, c0 + n1), W, ldw,
+                     at16(c.wh, c.ldh, r0, c0), at16(c.wl, c.ldh, r0, c0));
+}
+
+struct HLayout {
+  int* counters;
+  char* wh;
+  char* wl;
+  float* work32;
+  void* workh;
+  void* workl;
+  int64_t ldwk;
+  HrScratch hr;
+};
+
+bool carve_hou(Arena& ws, int m, int n, const Options& o, HLayout* L) {
+  const int64_t ldh = round_up(m, 8);
+  const bool split3 = o.prec == LATER_PREC_SPLIT3;
+  L->wh = reinterpret_cast<char*>(ws.take<uint16_t>(ldh * n));
+  L->wl = split3 ? reinterpret_cast<char*>(ws.take<uint16_t>(ldh * n)) : nullptr;
+  L->counters = ws.take<int>(kCounters);
+  const int n1 = n > 32 ? split_half(n) : 1;
+  const int n2 = std::max(n - n1, 1);
+  L->ldwk = round_up(n1, 8);
+  L->work32 = ws.take<float>(L->ldwk * n2);
+  L->workh = ws.take<uint16_t>(L->ldwk * n2);
+  L->workl = split3 ? ws.take<uint16_t>(L->ldwk * n2) : nullptr;
+  L->hr.U = ws.take<float>(32 * 32);
+  L->hr.T = ws.take<float>(32 * 32);
+  L->hr.s = ws.take<float>(32);
+  return !ws.failed();
+}
+
+}  // namespace
+
+QrNeed rhouqr_need(int m, int n, const Options& o) {
+  QrNeed q;
+  Arena a(nullptr, 0);
+  HLayout L;
+  carve_hou(a, m, n, o, &L);
+  const int64_t fixed = static_cast<int64_t>(a.peak() / sizeof(float)) + 64;
+  TsqrPlan plan{};
+  int ncnt;
+  int64_t stack;
+  tsqr_plan_sizes(m, &plan, &stack, &ncnt);
+  stack += 64 * kMaxTsqrLevels;
+  const int64_t parts = ((m + 127) / 128) * 4096LL * 4 + 128;  // up to 128 x 128 SIMT products
+  const int64_t splitk = static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 128;
+  q.min_work = fixed + std::max<int64_t>(stack, 4 * 4096 + 128);
+  q.rec_work = fixed + std::max(std::max(stack, parts), splitk);
+  q.hwork = round_up(m, 8) * n * (o.prec == LATER_PREC_SPLIT3 ? 2 : 1) + 64;
+  return q;
+}
+
+later_status_t rhouqr(cudaStream_t st, int m, int n, float* A, int64_t lda, float* W, int64_t ldw, float* R,
+                      int64_t ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
+  if (m < 1 || n < 1 || m < n || lda < m || ldw < m || ldr < n || !A || !W || !R) return LATER_ERR_INVALID_ARG;
+  if (n % 32 != 0) return LATER_ERR_INVALID_ARG;
+  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;
+  const QrNeed need = rhouqr_need(m, n, o);
+  if (!work || !hwork || lwork < need.min_work || lhwork < need.hwork) return LATER_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(hwork) & 15) != 0) return LATER_ERR_INVALID_ARG;
+  Arena ws(work, static_cast<size_t>(lwork) * sizeof(float));
+  HLayout L;
+  if (!carve_hou(ws, m, n, o, &L)) return LATER_ERR_WORKSPACE;
+  HCtx c;
+  c.st = st;
+  c.o = o;
+  c.ws = &ws;
+  c.counters = L.counters;
+  c.ldh = round_up(m, 8);
+  c.ah = static_cast<char*>(hwork);
+  c.al = o.prec == LATER_PREC_SPLIT3 ? c.ah + c.ldh * n * 2 : nullptr;
+  c.wh = L.wh;
+  c.wl = L.wl;
+  c.work32 = L.work32;
+  c.workh = L.workh;
+  c.workl = L.workl;
+  c.ldwk = L.ldwk;
+  c.hr = L.hr;
+  LATER_CHECK_CUDA(cudaMemsetAsync(L.counters, 0, kCounters * sizeof(int), st));
+  LATER_CHECK(fill_strict_lower(st, n, n, R, ldr, 0.f));
+  // 16-bit copy of the columns a tensor-core update will read before any
+  // kernel has rewritten them (all but the first leaf).
+  const int f = n > 32 ? first_leaf(n, 32) : n;
+  LATER_CHECK(convert16(st, m, n - f, A + static_cast<int64_t>(f) * lda, lda, c.ah + f * c.ldh * 2,
+                        c.al ? c.al + f * c.ldh * 2 : nullptr, c.ldh, o.prec));
+  return rec_hou(c, 0, m, 0, n, A, lda, W, ldw, R, ldr);
+}
+
+later_status_t ormqr(cudaStream_t st, int m, int n, float* W, int64_t ldw, const float* Y, int64_t ldy, float* work,
+                     int64_t lwork) {
+  if (m < 1 || n < 1 || m < n || ldw < m || ldy < m || !W || !Y) return LATER_ERR_INVALID_ARG;
+  if (!work || lwork < static_cast<int64_t>(m) * n) return LATER_ERR_WORKSPACE;
+  LATER_CHECK(form_q(st, m, n, W, ldw, Y, ldy, work, m));
+  return copy2d(st, m, n, work, m, W, ldw);
 }
 
 }  // namespace later

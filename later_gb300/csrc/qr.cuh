@@ -27,6 +27,15 @@ QrNeed rgsqrf_need(int m, int n, const Options& o);
 later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, float* R, int64_t ldr, float* work,
                       int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
 
+QrNeed rhouqr_need(int m, int n, const Options& o);
+
+later_status_t rhouqr(cudaStream_t st, int m, int n, float* A, int64_t lda, float* W, int64_t ldw, float* R,
+                      int64_t ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
+
+// Q = I - W Y^T (first n columns) written over W; `work` holds m x n floats.
+later_status_t ormqr(cudaStream_t st, int m, int n, float* W, int64_t ldw, const float* Y, int64_t ldy, float* work,
+                     int64_t lwork);
+
 // Split point of a width-n recursion step: the larger half, in 32-column units.
 inline int split_half(int n) { return ((n / 32 + 1) / 2) * 32; }
 

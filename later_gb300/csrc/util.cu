@@ -117,6 +117,16 @@ __global__ void copy2d_kernel(int m, int n, const float* X, int64_t ldx, float* 
     if (i < m) Y[i + static_cast<int64_t>(j) * ldy] = X[i + static_cast<int64_t>(j) * ldx];
 }
 
+__global__ void zero_block_kernel(int m, int n, float* X, int64_t ldx, uint16_t* xh, uint16_t* xl, int64_t ldh) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  for (int j = blockIdx.y; j < n; j += gridDim.y) {
+    X[i + static_cast<int64_t>(j) * ldx] = 0.f;
+    if (xh) xh[i + static_cast<int64_t>(j) * ldh] = 0;
+    if (xl) xl[i + static_cast<int64_t>(j) * ldh] = 0;
+  }
+}
+
 }  // namespace
 
 inline dim3 grid2d(int m, int n) {
@@ -144,6 +154,15 @@ later_status_t copy2d(cudaStream_t st, int m, int n, const float* X, int64_t ldx
   if (m <= 0 || n <= 0) return LATER_OK;
   TraceScope trace(st, TRACE_OTHER);
   copy2d_kernel<<<grid2d(m, n), 256, 0, st>>>(m, n, X, ldx, Y, ldy);
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+later_status_t zero_block(cudaStream_t st, int m, int n, float* X, int64_t ldx, void* xh, void* xl, int64_t ldh) {
+  if (m <= 0 || n <= 0) return LATER_OK;
+  TraceScope trace(st, TRACE_OTHER);
+  zero_block_kernel<<<grid2d(m, n), 256, 0, st>>>(m, n, X, ldx, static_cast<uint16_t*>(xh), static_cast<uint16_t*>(xl),
+                                                  ldh);
   note_launch();
   return cuda_status(cudaGetLastError());
 }

@@ -146,3 +146,93 @@ def rgsqrf(A: np.ndarray, leaf: int = 128, prec: str = "fp16", cgs2: bool = Fals
 
     rec(a, r)
     return a, r
+
+
+# ------------------------------------------------------------ Householder QR
+def householder_reconstruct(q: np.ndarray, r: np.ndarray, signs: bool = True):
+    """Compact-WY form of an explicit TSQR factor — reconstructY + leaf W,
+    QR/later_rhouqr.cu:56-78, 233-276.
+
+    LU without pivoting of (I - Q S): Y = L (unit lower trapezoidal), U upper;
+    W = (I - Q S) Y1^{-T} = Y T with T = U Y1^{-T}; R' = S R. With signs=True,
+    s_k = -sign of the k-th pivot candidate (Ballard et al., IPDPS 2014), which
+    makes every pivot >= 1 and gives LAPACK's Householder vectors; signs=False
+    is the reference's literal S = I (cusolverDnSgetrf on I - Q, :251-260).
+    """
+    q = np.array(q, dtype=F32)
+    m, k = q.shape
+    g = q[:k, :].copy()
+    L = np.eye(k, dtype=F32)
+    U = np.zeros((k, k), dtype=F32)
+    s = np.ones(k, dtype=F32)
+    for j in range(k):
+        # eliminate column j with the previous pivots (lower part of L known)
+        col = g[:, j].copy()
+        for i in range(j):
+            col[i + 1:] -= L[i + 1:, i] * col[i]
+        gk = col[j]
+        sj = F32(-1.0 if gk >= 0 else 1.0) if signs else F32(1.0)
+        s[j] = sj
+        v = -sj * col
+        v[j] += F32(1.0)
+        U[: j + 1, j] = v[: j + 1]
+        L[j + 1:, j] = v[j + 1:] / v[j]
+        g[:, j] = col
+    y = np.zeros((m, k), dtype=F32)
+    y[:k] = np.tril(L)
+    # bottom rows: y U = -(q S)
+    b = -(q[k:] * s[None, :])
+    y[k:] = np.linalg.solve(U.T.astype(np.float64), b.T.astype(np.float64)).T.astype(F32)
+    t = (U.astype(np.float64) @ np.linalg.inv(np.tril(L).astype(np.float64)).T).astype(F32)
+    t = np.triu(t)
+    w = (y @ t).astype(F32)
+    return y, w, (s[:, None] * np.asarray(r, dtype=F32)).astype(F32), t
+
+
+def rhouqr(A: np.ndarray, prec: str = "fp16", signs: bool = True):
+    """Recursive Householder QR — later_rhouqr / qr, QR/later_rhouqr.cu:27-201.
+
+    Returns (Y, W, R) with Q = I - W Y^T. Leaf n <= 32: TSQR then Householder
+    reconstruction. Trailing update A2 <- (I - Y1 W1^T) A2 and the W merge
+    W2 <- W2 - W1 (Y1^T W2) run in FP32 when n/2 <= 128 or m <= 128 (:83-102),
+    else with FP16-rounded operands (:104-135). The top n/2 rows of W2 are
+    zero before the merge.
+    """
+    a = np.array(A, dtype=F32, order="F")
+    m, n = a.shape
+    w = np.zeros((m, n), dtype=F32)
+    r = np.zeros((n, n), dtype=F32)
+
+    def gemm(x, y, use_tc):
+        return tc_gemm(x, y, prec) if use_tc else (x @ y).astype(F32)
+
+    def rec(a, w, r):
+        mr, nn = a.shape
+        if nn <= 32:
+            q, rr = tsqr32(a)
+            y, ww, rr2, _ = householder_reconstruct(q, rr, signs)
+            a[:] = y
+            w[:] = ww
+            r[:nn, :nn] = rr2
+            return
+        n1 = split_half(nn)
+        rec(a[:, :n1], w[:, :n1], r[:n1, :n1])
+        tc = n1 > 128 and mr > 128
+        work = gemm(w[:, :n1].T, a[:, n1:], tc)
+        a[:, n1:] -= gemm(a[:, :n1], work, tc)
+        rec(a[n1:, n1:], w[n1:, n1:], r[n1:, n1:])
+        r[:n1, n1:] = a[:n1, n1:]
+        a[:n1, n1:] = 0
+        w[:n1, n1:] = 0
+        work = gemm(a[:, :n1].T, w[:, n1:], tc)
+        w[:, n1:] -= gemm(w[:, :n1], work, tc)
+
+    rec(a, w, r)
+    return a, w, r
+
+
+def ormqr(W: np.ndarray, Y: np.ndarray) -> np.ndarray:
+    """Q = I - W Y1^T (first n columns) — QR/later_ormqr.cu:50-58, in FP32."""
+    m, n = W.shape
+    y1 = np.tril(np.asarray(Y, dtype=F32)[:n, :n], -1) + np.eye(n, dtype=F32)
+    return (np.eye(m, n, dtype=F32) - W.astype(F32) @ y1.T).astype(F32)
