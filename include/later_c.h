@@ -104,6 +104,56 @@ later_status_t later_c_rhouqr(later_stream_t stream, int m, int n, float* A, int
 later_status_t later_c_ormqr(later_stream_t stream, int m, int n, float* W, int ldw, const float* Y, int ldy,
                              float* work, int64_t lwork);
 
+/* ------------------------------------------------- BLAS-3 and Cholesky */
+
+/*
+ * Workspace of the BLAS-3 / Cholesky routines: `hwork` (16-bit elements) is
+ * required; `work` (floats) is optional and lets the tensor-core GEMMs split
+ * K over idle SMs. `op` is 's' (rsyrk: m = n, n = k), 't' (rtrsm, leri in
+ * `side`), 'm' (rtrmm) or 'p' (rpotrf: m = n).
+ */
+later_status_t later_c_blas3_bufsize(char op, char side, int m, int n, const later_options_t* opt, int64_t* lwork,
+                                     int64_t* lhwork);
+
+/*
+ * C <- alpha A A^T + beta C on the lower triangle (C n x n, A n x k).
+ * Replaces LATER include/LATER.h:62 later_rsyrk (BLAS/later_rsyrk.cu:12-93).
+ * The strictly upper triangle of C is not referenced.
+ */
+later_status_t later_c_rsyrk(later_stream_t stream, int n, int k, float alpha, const float* A, int lda, float beta,
+                             float* C, int ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                             const later_options_t* opt);
+
+/*
+ * Triangular solve with a lower-triangular A, in place in B:
+ *   ('l','l','n'): A X = B, A m x m;   ('l','r','t'): X A^T = B, A n x n.
+ * Replaces LATER include/LATER.h:60 later_rtrsm (BLAS/later_rtrsm.cu:165-187).
+ * Other flag combinations return LATER_ERR_NOT_SUPPORTED (the reference
+ * silently did nothing).
+ */
+later_status_t later_c_rtrsm(later_stream_t stream, char uplo, char leri, char trans, int m, int n, const float* A,
+                             int lda, float* B, int ldb, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                             const later_options_t* opt);
+
+/*
+ * C = A B with A m x m lower triangular, B and C m x n.
+ * Replaces LATER include/LATER.h:64 later_rtrmm (BLAS/later_rtrmm.cu:14-86);
+ * the reference's tempC scratch is not needed (the off-diagonal product is
+ * accumulated into C by the GEMM epilogue).
+ */
+later_status_t later_c_rtrmm(later_stream_t stream, int m, int n, const float* A, int lda, const float* B, int ldb,
+                             float* C, int ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                             const later_options_t* opt);
+
+/*
+ * Lower Cholesky factor in place: A = L L^T (uplo 'l' only), any lda >= n.
+ * Replaces LATER include/LATER.h:80 later_rpotrf (Cholesky/later_rpotrf.cu:68-91).
+ * A non-positive pivot is reported by later_c_device_status as
+ * LATER_ERR_NUMERIC. The strictly upper triangle of A is not referenced.
+ */
+later_status_t later_c_rpotrf(later_stream_t stream, char uplo, int n, float* A, int lda, float* work,
+                              int64_t lwork, void* hwork, int64_t lhwork, const later_options_t* opt);
+
 /* --------------------------------------------------------- building blocks */
 
 /*

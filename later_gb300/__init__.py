@@ -19,7 +19,8 @@ from . import build as _build
 
 __all__ = [
     "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
-    "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
+    "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "later_rsyrk", "later_rtrsm",
+    "later_rtrmm", "later_rpotrf", "blas3_bufsize", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
     "trace_end",
 ]
 
@@ -59,6 +60,13 @@ _SIGS = {
     "later_c_rhouqr_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "later_c_rhouqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_ormqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i64]),
+    "later_c_blas3_bufsize": (_i, [ctypes.c_char, ctypes.c_char, _i, _i, ctypes.POINTER(Options),
+                                   ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "later_c_rsyrk": (_i, [_vp, _i, _i, _f, _vp, _i, _f, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
+    "later_c_rtrsm": (_i, [_vp, ctypes.c_char, ctypes.c_char, ctypes.c_char, _i, _i, _vp, _i, _vp, _i, _vp, _i64,
+                           _vp, _i64, ctypes.POINTER(Options)]),
+    "later_c_rtrmm": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
+    "later_c_rpotrf": (_i, [_vp, ctypes.c_char, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_launch_count": (ctypes.c_uint64, []),
     "later_c_trace_begin": (None, []),
     "later_c_trace_end": (_i, [_vp]),
@@ -220,6 +228,63 @@ def later_ormqr(W, Y, work=None, stream=None):
     _check(lib().later_c_ormqr(_stream(stream), m, n, W.data_ptr(), _ld(W, "W"), Y.data_ptr(), _ld(Y, "Y"),
                                work.data_ptr(), work.numel()), "later_ormqr")
     return W
+
+
+def blas3_bufsize(op, m, n, side="l", precision="fp16"):
+    o = Options.make(precision)
+    lw, lh = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().later_c_blas3_bufsize(op.encode(), side.encode(), m, n, ctypes.byref(o), ctypes.byref(lw),
+                                       ctypes.byref(lh)), "blas3_bufsize")
+    return lw.value, lh.value
+
+
+def _b3_ws(op, m, n, side, precision, device, work, hwork):
+    import torch
+    lw, lh = blas3_bufsize(op, m, n, side, precision)
+    if work is None:
+        work = torch.empty(lw, dtype=torch.float32, device=device)
+    if hwork is None:
+        hwork = torch.empty(max(lh, 8), dtype=torch.float16, device=device)
+    return work, hwork
+
+
+def later_rsyrk(n, k, alpha, A, beta, C, *, precision="fp16", work=None, hwork=None, stream=None):
+    """C <- alpha A A^T + beta C, lower triangle (include/LATER.h:62)."""
+    work, hwork = _b3_ws("s", n, k, "l", precision, C.device, work, hwork)
+    o = Options.make(precision)
+    _check(lib().later_c_rsyrk(_stream(stream), n, k, alpha, A.data_ptr(), _ld(A, "A"), beta, C.data_ptr(),
+                               _ld(C, "C"), work.data_ptr(), work.numel(), hwork.data_ptr(), hwork.numel(),
+                               ctypes.byref(o)), "later_rsyrk")
+    return C
+
+
+def later_rtrsm(uplo, leri, trans, m, n, A, B, *, precision="fp16", work=None, hwork=None, stream=None):
+    """In-place triangular solve, ('l','l','n') or ('l','r','t') (include/LATER.h:60)."""
+    work, hwork = _b3_ws("t", m, n, leri, precision, B.device, work, hwork)
+    o = Options.make(precision)
+    _check(lib().later_c_rtrsm(_stream(stream), uplo.encode(), leri.encode(), trans.encode(), m, n, A.data_ptr(),
+                               _ld(A, "A"), B.data_ptr(), _ld(B, "B"), work.data_ptr(), work.numel(),
+                               hwork.data_ptr(), hwork.numel(), ctypes.byref(o)), "later_rtrsm")
+    return B
+
+
+def later_rtrmm(m, n, A, B, C, *, precision="fp16", work=None, hwork=None, stream=None):
+    """C = A B, A lower triangular (include/LATER.h:64)."""
+    work, hwork = _b3_ws("m", m, n, "l", precision, C.device, work, hwork)
+    o = Options.make(precision)
+    _check(lib().later_c_rtrmm(_stream(stream), m, n, A.data_ptr(), _ld(A, "A"), B.data_ptr(), _ld(B, "B"),
+                               C.data_ptr(), _ld(C, "C"), work.data_ptr(), work.numel(), hwork.data_ptr(),
+                               hwork.numel(), ctypes.byref(o)), "later_rtrmm")
+    return C
+
+
+def later_rpotrf(uplo, n, A, *, precision="fp16", work=None, hwork=None, stream=None):
+    """Lower Cholesky in place (include/LATER.h:80)."""
+    work, hwork = _b3_ws("p", n, n, "l", precision, A.device, work, hwork)
+    o = Options.make(precision)
+    _check(lib().later_c_rpotrf(_stream(stream), uplo.encode(), n, A.data_ptr(), _ld(A, "A"), work.data_ptr(),
+                                work.numel(), hwork.data_ptr(), hwork.numel(), ctypes.byref(o)), "later_rpotrf")
+    return A
 
 
 def gemm16(transa, transb, A, B, alpha=1.0, beta=0.0, C=None, D=None, precision="fp16", work=None, stream=None):

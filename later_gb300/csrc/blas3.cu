@@ -1,0 +1,487 @@
+// Recursive BLAS-3 (rsyrk, rtrsm, rtrmm) and recursive Cholesky (rpotrf).
+//
+// Reference structure (all split the dimension in half and run the
+// off-diagonal product as an FP16 cublasGemmEx on s2h copies):
+//   later_rsyrk  BLAS/later_rsyrk.cu:12-93   leaf n <= 2048: full square GemmEx
+//   later_rtrsm  BLAS/later_rtrsm.cu:75-187  leaf <= 256: cublasStrsm; only
+//                ('l','l','n') and ('l','r','t'); other flags are a silent no-op
+//   later_rtrmm  BLAS/later_rtrmm.cu:14-86   leaf <= 256: cublasStrmm; GemmEx
+//                into tempC, then cublasSgeam C2 += tempC
+//   later_rpotrf Cholesky/later_rpotrf.cu:22-91 leaf <= 2048: cusolverDnSpotrf,
+//                off-diagonal later_rtrsm('l','r','t'), trailing later_rsyrk
+// Here:
+//   * rsyrk is one tensor-core NT launch over the lower tiles only (tiles above
+//     the diagonal exit at once), alpha / beta in the epilogue;
+//   * the leaves are FP32 kernels of this file (substitution TRSM, TRMM, and a
+//     one-CTA Cholesky with a pivot check that reports LATER_ERR_NUMERIC);
+//   * rtrmm adds L21 B1 into C2 in the GEMM epilogue (beta = 1): no tempC;
+//   * 16-bit operand copies are written by the producing leaf (solved X) or
+//     converted once per operand block right before its GEMM;
+//   * leading dimensions are honoured (the reference's rpotrf assumes lda == n).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "blas3.cuh"
+#include "panel.cuh"
+#include "runtime.cuh"
+
+namespace later {
+
+namespace {
+
+constexpr int NB = 128;  // leaf size of the triangular solves / products / Cholesky
+// Below these sizes the reference runs pure FP32 (cublasStrsm / cublasStrmm
+// leaves of 256, BLAS/later_rtrsm.cu:5, BLAS/later_rtrmm.cu:5; cuSOLVER Spotrf
+// leaves of 2048, Cholesky/later_rpotrf.cu:7): the recursion below them uses
+// FP32 SIMT updates instead of tensor-core ones.
+constexpr int kFp32Trsm = 256;
+constexpr int kFp32Potrf = 2048;
+
+__device__ __forceinline__ void put16(void* hi, void* lo, int64_t o, float v, int mode) {
+  if (!hi) return;
+  if (mode == 1) {
+    reinterpret_cast<__nv_bfloat16*>(hi)[o] = __float2bfloat16_rn(v);
+  } else {
+    const __half h = __float2half_rn(v);
+    reinterpret_cast<__half*>(hi)[o] = h;
+    if (mode == 2) reinterpret_cast<__half*>(lo)[o] = __float2half_rn((v - __half2float(h)) * 2048.f);
+  }
+}
+
+// X L^T = B (right, lower, transposed), L nb x nb (nb <= 128), B m x nb. One
+// thread per row of B; L and the rows being solved live in shared memory.
+__global__ void __launch_bounds__(128) trsm_rlt_leaf(int m, int nb, const float* __restrict__ L, int64_t ldl,
+                                                     float* B, int64_t ldb, void* xh, void* xl, int64_t ldh,
+                                                     int mode) {
+  extern __shared__ float sm[];
+  float* Ls = sm;                // [nb][129]  Ls[j*129 + i] = L[j][i]
+  float* Xs = sm + NB * 129;     // [128 rows][129]
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int j = e % nb, i = e / nb;
+    Ls[j * 129 + i] = (i <= j) ? L[j + static_cast<int64_t>(i) * ldl] : 0.f;
+  }
+  const int r0 = blockIdx.x * 128;
+  const int row = r0 + threadIdx.x;
+  const bool in = row < m;
+  for (int j = 0; j < nb; ++j) Xs[threadIdx.x * 129 + j] = in ? B[row + static_cast<int64_t>(j) * ldb] : 0.f;
+  __syncthreads();
+  if (!in) return;
+  float* x = Xs + threadIdx.x * 129;
+  for (int j = 0; j < nb; ++j) {
+    float acc = x[j];
+    const float* lj = Ls + j * 129;
+    for (int i = 0; i < j; ++i) acc -= x[i] * lj[i];
+    acc /= lj[j];
+    x[j] = acc;
+    B[row + static_cast<int64_t>(j) * ldb] = acc;
+    put16(xh, xl, row + static_cast<int64_t>(j) * ldh, acc, mode);
+  }
+}
+
+// L X = B (left, lower, no transpose), L nb x nb (nb <= 128), B nb x n. One
+// CTA per 32 columns of B staged in shared memory; one thread per column.
+__global__ void __launch_bounds__(32) trsm_lln_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl, float* B,
+                                                    int64_t ldb, void* xh, void* xl, int64_t ldh, int mode) {
+  extern __shared__ float sm[];
+  float* Ls = sm;             // [i][k] at i*129 + k
+  float* Bs = sm + NB * 129;  // [col][row] at c*129 + r
+  const int c0 = blockIdx.x * 32;
+  for (int e = threadIdx.x; e < nb * nb; e += 32) {
+    const int i = e % nb, k = e / nb;
+    Ls[i * 129 + k] = (k <= i) ? L[i + static_cast<int64_t>(k) * ldl] : 0.f;
+  }
+  for (int c = 0; c < 32; ++c)
+    for (int r = threadIdx.x; r < nb; r += 32)
+      Bs[c * 129 + r] = (c0 + c < n) ? B[r + static_cast<int64_t>(c0 + c) * ldb] : 0.f;
+  __syncthreads();
+  float* x = Bs + threadIdx.x * 129;
+  for (int i = 0; i < nb; ++i) {
+    float acc = x[i];
+    const float* li = Ls + i * 129;
+    for (int k = 0; k < i; ++k) acc -= li[k] * x[k];
+    x[i] = acc / li[i];
+  }
+  __syncthreads();
+  for (int c = 0; c < 32; ++c) {
+    if (c0 + c >= n) break;
+    for (int r = threadIdx.x; r < nb; r += 32) {
+      const float v = Bs[c * 129 + r];
+      B[r + static_cast<int64_t>(c0 + c) * ldb] = v;
+      put16(xh, xl, r + static_cast<int64_t>(c0 + c) * ldh, v, mode);
+    }
+  }
+}
+
+// C = L B (left, lower), L nb x nb (nb <= 128), B nb x n, C nb x n. One CTA
+// per 64 columns; each thread accumulates 8 rows x 4 columns... of its share.
+__global__ void __launch_bounds__(256) trmm_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl,
+                                                 const float* __restrict__ B, int64_t ldb, float* C, int64_t ldc) {
+  extern __shared__ float sm[];
+  float* Ls = sm;             // [i][k]
+  float* Bs = sm + NB * 129;  // [k][c] at k*65 + c
+  const int c0 = blockIdx.x * 64;
+  for (int e = threadIdx.x; e < nb * nb; e += 256) {
+    const int i = e % nb, k = e / nb;
+    Ls[i * 129 + k] = (k <= i) ? L[i + static_cast<int64_t>(k) * ldl] : 0.f;
+  }
+  for (int e = threadIdx.x; e < nb * 64; e += 256) {
+    const int k = e % nb, c = e / nb;
+    Bs[k * 65 + c] = (c0 + c < n) ? B[k + static_cast<int64_t>(c0 + c) * ldb] : 0.f;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nb * 64; e += 256) {
+    const int i = e % nb, c = e / nb;
+    if (c0 + c >= n) continue;
+    float acc = 0.f;
+    for (int k = 0; k <= i; ++k) acc += Ls[i * 129 + k] * Bs[k * 65 + c];
+    C[i + static_cast<int64_t>(c0 + c) * ldc] = acc;
+  }
+}
+
+// Lower Cholesky of an nb x nb block (nb <= 128) in one CTA, in shared memory.
+// Right-looking; a non-positive (or NaN) pivot sets DEV_NUMERIC and the
+// factorisation continues with pivot 1 so the kernel always finishes.
+__global__ void __launch_bounds__(1024) potrf_leaf(int nb, float* A, int64_t lda, int* status) {
+  extern __shared__ float sm[];
+  float* As = sm;  // [i][j] at i*129 + j (lower part used)
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e % nb, j = e / nb;
+    if (i >= j) As[i * 129 + j] = A[i + static_cast<int64_t>(j) * lda];
+  }
+  __shared__ float piv;
+  __syncthreads();
+  for (int k = 0; k < nb; ++k) {
+    if (threadIdx.x == 0) {
+      float d = As[k * 129 + k];
+      if (!(d > 0.f)) {
+        report(status, DEV_NUMERIC);
+        d = 1.f;
+      }
+      piv = sqrtf(d);
+      As[k * 129 + k] = piv;
+    }
+    __syncthreads();
+    const float inv = 1.f / piv;
+    for (int i = k + 1 + threadIdx.x; i < nb; i += blockDim.x) As[i * 129 + k] *= inv;
+    __syncthreads();
+    const int t = nb - k - 1;  // trailing size; update the lower triangle of it
+    for (int e = threadIdx.x; e < t * t; e += blockDim.x) {
+      const int i = k + 1 + e % t, j = k + 1 + e / t;
+      if (i >= j) As[i * 129 + j] -= As[i * 129 + k] * As[j * 129 + k];
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e % nb, j = e / nb;
+    if (i >= j) A[i + static_cast<int64_t>(j) * lda] = As[i * 129 + j];
+  }
+}
+
+inline int mode_of(int prec) { return prec == LATER_PREC_BF16 ? 1 : (prec == LATER_PREC_SPLIT3 ? 2 : 0); }
+
+// Splits n in half, rounded to a multiple of 64 (keeps 16-bit row offsets
+// 16-byte aligned for the tensor maps).
+inline int half64(int n) { return std::max(64, static_cast<int>(round_up(n / 2, 64))); }
+
+bool smem_attr(const void* fn, size_t bytes) {
+  static bool done[8][64] = {};
+  static const void* fns[8] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int slot = 0;
+  for (; slot < 8; ++slot)
+    if (fns[slot] == fn || fns[slot] == nullptr) break;
+  if (slot == 8 || dev >= 64) return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          static_cast<int>(bytes)) == cudaSuccess;
+  fns[slot] = fn;
+  if (!done[slot][dev]) {
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)) != cudaSuccess)
+      return false;
+    done[slot][dev] = true;
+  }
+  return true;
+}
+
+struct B3 {
+  cudaStream_t st;
+  Options o;
+  char* h;      // 16-bit scratch (hwork) cursor
+  size_t hcap;  // bytes
+  Scratch sc;   // split-K scratch
+};
+
+// Takes `elems` 16-bit elements from the hwork scratch (256-byte aligned).
+char* take16(B3& b, int64_t elems, size_t* mark) {
+  const uintptr_t p = (reinterpret_cast<uintptr_t>(b.h) + 255) & ~uintptr_t(255);
+  const size_t used = p - reinterpret_cast<uintptr_t>(b.h);
+  const size_t need = used + static_cast<size_t>(elems) * 2 * (b.o.prec == LATER_PREC_SPLIT3 ? 2 : 1);
+  if (need > b.hcap) return nullptr;
+  *mark = need;
+  return reinterpret_cast<char*>(p);
+}
+
+// 16-bit copy of an m x n FP32 block into the scratch (hi, and lo for SPLIT3).
+later_status_t copy16(B3& b, int m, int n, const float* X, int64_t ldx, Op16* out, size_t* used) {
+  const int64_t ld = round_up(m, 8);
+  size_t mark = 0;
+  char* p = take16(b, ld * n, &mark);
+  if (!p) return LATER_ERR_WORKSPACE;
+  out->hi = p;
+  out->lo = b.o.prec == LATER_PREC_SPLIT3 ? p + ld * n * 2 : nullptr;
+  out->ld = ld;
+  *used = mark;
+  return convert16(b.st, m, n, X, ldx, const_cast<void*>(out->hi), const_cast<void*>(out->lo), ld, b.o.prec);
+}
+
+later_status_t gemm(B3& b, char ta, char tb, int M, int N, int K, float alpha, const Op16& A, const Op16& Bm,
+                    float beta, float* C, int64_t ldc, void* dh = nullptr, void* dl = nullptr, int64_t ldh = 0,
+                    int lower = 0) {
+  GemmCall g;
+  g.ta = ta;
+  g.tb = tb;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.A = A;
+  g.B = Bm;
+  g.alpha = alpha;
+  g.beta = beta;
+  g.out.C = C;
+  g.out.ldc = ldc;
+  g.out.D = C;
+  g.out.ldd = ldc;
+  g.out.Dh = dh;
+  g.out.Dl = dl;
+  g.out.ldh = ldh;
+  g.out.lower = lower;
+  g.prec = b.o.prec;
+  g.out_prec = b.o.prec;
+  return tc_gemm(g, b.sc, b.st, b.o.budget);
+}
+
+// -------------------------------------------------------------- recursions
+// X L^T = B, L n x n, B m x n. X's 16-bit copy goes to (xh, ldh) (columns as B).
+// Updates are FP32 while n <= fp32_lim, tensor-core above.
+later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float* B, int64_t ldb, char* xh, char* xl,
+                        int64_t ldh, int fp32_lim = kFp32Trsm) {
+  if (n <= NB) {
+    const size_t smem = (NB * 129 + 128 * 129) * sizeof(float);
+    if (!smem_attr(reinterpret_cast<const void*>(trsm_rlt_leaf), smem)) return LATER_ERR_CUDA;
+    TraceScope tr(b.st, TRACE_OTHER);
+    trsm_rlt_leaf<<<(m + 127) / 128, 128, smem, b.st>>>(m, n, L, ldl, B, ldb, xh, xl, ldh, mode_of(b.o.prec));
+    note_launch();
+    return cuda_status(cudaGetLastError());
+  }
+  const int n1 = half64(n), n2 = n - n1;
+  LATER_CHECK(trsm_rlt(b, m, n1, L, ldl, B, ldb, xh, xl, ldh, fp32_lim));
+  // B2 -= X1 L21^T   (L21 = L[n1:, :n1], n2 x n1)
+  if (n <= fp32_lim) {
+    LATER_CHECK(simt_gemm_acc(b.st, m, n1, n2, -1.f, B, ldb, L + n1, ldl, 1, 0, B + n1 * ldb, ldb));
+  } else {
+    B3 sub = b;
+    Op16 l21;
+    size_t used = 0;
+    LATER_CHECK(copy16(sub, n2, n1, L + n1, ldl, &l21, &used));
+    sub.h += used;
+    sub.hcap -= used;
+    const Op16 x1{xh, xl, ldh};
+    LATER_CHECK(gemm(sub, 'N', 'T', m, n2, n1, -1.f, x1, l21, 1.f, B + n1 * ldb, ldb));
+  }
+  return trsm_rlt(b, m, n2, L + n1 + n1 * ldl, ldl, B + n1 * ldb, ldb, xh ? xh + n1 * ldh * 2 : nullptr,
+                  xl ? xl + n1 * ldh * 2 : nullptr, ldh, fp32_lim);
+}
+
+// L X = B, L m x m, B m x n. X's 16-bit copy goes to (xh, ldh) (rows as B).
+later_status_t trsm_lln(B3& b, int m, int n, const float* L, int64_t ldl, float* B, int64_t ldb, char* xh, char* xl,
+                        int64_t ldh, int fp32_lim = kFp32Trsm) {
+  if (m <= NB) {
+    const size_t smem = (NB * 129 + 32 * 129) * sizeof(float);
+    if (!smem_attr(reinterpret_cast<const void*>(trsm_lln_leaf), smem)) return LATER_ERR_CUDA;
+    TraceScope tr(b.st, TRACE_OTHER);
+    trsm_lln_leaf<<<(n + 31) / 32, 32, smem, b.st>>>(m, n, L, ldl, B, ldb, xh, xl, ldh, mode_of(b.o.prec));
+    note_launch();
+    return cuda_status(cudaGetLastError());
+  }
+  const int m1 = half64(m), m2 = m - m1;
+  LATER_CHECK(trsm_lln(b, m1, n, L, ldl, B, ldb, xh, xl, ldh, fp32_lim));
+  // B2 -= L21 X1   (L21 = L[m1:, :m1], m2 x m1)
+  if (m <= fp32_lim) {
+    LATER_CHECK(simt_gemm_acc(b.st, m2, m1, n, -1.f, L + m1, ldl, B, ldb, 0, 0, B + m1, ldb));
+  } else {
+    B3 sub = b;
+    Op16 l21;
+    size_t used = 0;
+    LATER_CHECK(copy16(sub, m2, m1, L + m1, ldl, &l21, &used));
+    sub.h += used;
+    sub.hcap -= used;
+    const Op16 x1{xh, xl, ldh};
+    LATER_CHECK(gemm(sub, 'N', 'N', m2, n, m1, -1.f, l21, x1, 1.f, B + m1, ldb));
+  }
+  return trsm_lln(b, m2, n, L + m1 + m1 * ldl, ldl, B + m1, ldb, xh ? xh + m1 * 2 : nullptr,
+                  xl ? xl + m1 * 2 : nullptr, ldh, fp32_lim);
+}
+
+// C = L B, L m x m lower, B m x n (its 16-bit copy bh, ldbh), C m x n.
+later_status_t trmm_rec(B3& b, int m, int n, const float* L, int64_t ldl, const float* B, int64_t ldb, const Op16& bh,
+                        float* C, int64_t ldc) {
+  if (m <= NB) {
+    const size_t smem = (NB * 129 + NB * 65) * sizeof(float);
+    if (!smem_attr(reinterpret_cast<const void*>(trmm_leaf), smem)) return LATER_ERR_CUDA;
+    TraceScope tr(b.st, TRACE_OTHER);
+    trmm_leaf<<<(n + 63) / 64, 256, smem, b.st>>>(m, n, L, ldl, B, ldb, C, ldc);
+    note_launch();
+    return cuda_status(cudaGetLastError());
+  }
+  const int m1 = half64(m), m2 = m - m1;
+  LATER_CHECK(trmm_rec(b, m1, n, L, ldl, B, ldb, bh, C, ldc));
+  Op16 bh2{bh.hi ? static_cast<const char*>(bh.hi) + m1 * 2 : nullptr,
+           bh.lo ? static_cast<const char*>(bh.lo) + m1 * 2 : nullptr, bh.ld};
+  LATER_CHECK(trmm_rec(b, m2, n, L + m1 + m1 * ldl, ldl, B + m1, ldb, bh2, C + m1, ldc));
+  // C2 += L21 B1
+  if (m <= kFp32Trsm) return simt_gemm_acc(b.st, m2, m1, n, 1.f, L + m1, ldl, B, ldb, 0, 0, C + m1, ldc);
+  B3 sub = b;
+  Op16 l21;
+  size_t used = 0;
+  LATER_CHECK(copy16(sub, m2, m1, L + m1, ldl, &l21, &used));
+  sub.h += used;
+  sub.hcap -= used;
+  return gemm(sub, 'N', 'N', m2, n, m1, 1.f, l21, bh, 1.f, C + m1, ldc);
+}
+
+later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda) {
+  if (n <= NB) {
+    const size_t smem = NB * 129 * sizeof(float);
+    if (!smem_attr(reinterpret_cast<const void*>(potrf_leaf), smem)) return LATER_ERR_CUDA;
+    TraceScope tr(b.st, TRACE_PANEL);
+    potrf_leaf<<<1, 1024, smem, b.st>>>(n, A, lda, device_status_ptr());
+    note_launch();
+    return cuda_status(cudaGetLastError());
+  }
+  const int n1 = half64(n), n2 = n - n1;
+  LATER_CHECK(potrf_rec(b, n1, A, lda));
+  const bool fp32 = n <= kFp32Potrf;
+  // A21 <- A21 L11^{-T}; its 16-bit copy is written by the solve.
+  const int64_t ldx = round_up(n2, 8);
+  size_t used = 0;
+  char* xh = fp32 ? nullptr : take16(b, ldx * n1, &used);
+  if (!fp32 && !xh) return LATER_ERR_WORKSPACE;
+  char* xl = (xh && b.o.prec == LATER_PREC_SPLIT3) ? xh + ldx * n1 * 2 : nullptr;
+  B3 sub = b;
+  sub.h += used;
+  sub.hcap -= used;
+  LATER_CHECK(trsm_rlt(sub, n2, n1, A, lda, A + n1, lda, xh, xl, ldx, fp32 ? n1 : kFp32Trsm));
+  // A22 <- A22 - A21 A21^T (lower triangle only)
+  if (fp32) {
+    LATER_CHECK(simt_gemm_acc(b.st, n2, n1, n2, -1.f, A + n1, lda, A + n1, lda, 1, 1, A + n1 + n1 * lda, lda));
+  } else {
+    const Op16 x{xh, xl, ldx};
+    LATER_CHECK(gemm(sub, 'N', 'T', n2, n2, n1, -1.f, x, x, 1.f, A + n1 + n1 * lda, lda, nullptr, nullptr, 0, 1));
+  }
+  return potrf_rec(b, n2, A + n1 + n1 * lda, lda);
+}
+
+B3 make_b3(cudaStream_t st, const Options& o, float* work, int64_t lwork, void* hwork, int64_t lhwork) {
+  B3 b;
+  b.st = st;
+  b.o = o;
+  b.h = static_cast<char*>(hwork);
+  b.hcap = static_cast<size_t>(std::max<int64_t>(lhwork, 0)) * 2;
+  if (work && lwork > 4096) {
+    b.sc.partial = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(work) + 255) & ~uintptr_t(255));
+    b.sc.partial_floats = lwork - 128;
+    b.sc.counters = nullptr;
+    b.sc.n_counters = 1 << 20;  // split-K needs no counters (separate reduction kernel)
+  }
+  return b;
+}
+
+inline int64_t mult(const Options& o) { return o.prec == LATER_PREC_SPLIT3 ? 2 : 1; }
+
+}  // namespace
+
+// ------------------------------------------------------------ entry points
+int64_t rsyrk_hwork(int n, int k, const Options& o) { return (round_up(n, 8) * k + 256) * mult(o); }
+int64_t rtrsm_hwork(int m, int n, char leri, const Options& o) {
+  // X copy (B-sized) + the largest L21 block
+  const int64_t x = round_up(m, 8) * n;
+  const int64_t t = (leri == 'r' || leri == 'R') ? static_cast<int64_t>(n) : static_cast<int64_t>(m);
+  const int64_t h = t / 2 + 64;
+  return (x + round_up(h, 8) * h + 1024) * mult(o);
+}
+int64_t rtrmm_hwork(int m, int n, const Options& o) {
+  const int64_t h = m / 2 + 64;
+  return (round_up(m, 8) * n + round_up(h, 8) * h + 1024) * mult(o);
+}
+int64_t rpotrf_hwork(int n, const Options& o) {
+  const int64_t h = n / 2 + 64;
+  return (round_up(h, 8) * h + round_up(h / 2 + 64, 8) * (h / 2 + 64) + 2048) * mult(o);
+}
+int64_t splitk_work() { return static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 256; }
+
+later_status_t rsyrk(cudaStream_t st, int n, int k, float alpha, const float* A, int64_t lda, float beta, float* C,
+                     int64_t ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
+  if (n < 0 || k < 0 || lda < std::max(n, 1) || ldc < std::max(n, 1) || !A || !C) return LATER_ERR_INVALID_ARG;
+  if (n == 0) return LATER_OK;
+  if (!hwork || lhwork < rsyrk_hwork(n, k, o) || (reinterpret_cast<uintptr_t>(hwork) & 15)) return LATER_ERR_WORKSPACE;
+  B3 b = make_b3(st, o, work, lwork, hwork, lhwork);
+  if (k == 0) return axpy2d(st, n, n, beta - 1.f, C, ldc, C, ldc);  // C = beta C (lower and upper alike)
+  Op16 a;
+  size_t used = 0;
+  LATER_CHECK(copy16(b, n, k, A, lda, &a, &used));
+  return gemm(b, 'N', 'T', n, n, k, alpha, a, a, beta, C, ldc, nullptr, nullptr, 0, 1);
+}
+
+later_status_t rtrsm(cudaStream_t st, char uplo, char leri, char trans, int m, int n, const float* A, int64_t lda,
+                     float* B, int64_t ldb, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                     const Options& o) {
+  auto lc = [](char c) { return static_cast<char>(c | 0x20); };
+  const char u = lc(uplo), s = lc(leri), t = lc(trans);
+  const bool lln = (u == 'l' && s == 'l' && t == 'n');
+  const bool lrt = (u == 'l' && s == 'r' && t == 't');
+  if (!lln && !lrt) return LATER_ERR_NOT_SUPPORTED;
+  if (m < 0 || n < 0 || !A || !B || ldb < std::max(m, 1) || lda < std::max(lln ? m : n, 1)) return LATER_ERR_INVALID_ARG;
+  if (m == 0 || n == 0) return LATER_OK;
+  if (!hwork || lhwork < rtrsm_hwork(m, n, s, o) || (reinterpret_cast<uintptr_t>(hwork) & 15))
+    return LATER_ERR_WORKSPACE;
+  B3 b = make_b3(st, o, work, lwork, hwork, lhwork);
+  const int64_t ldx = round_up(m, 8);
+  size_t used = 0;
+  char* xh = take16(b, ldx * n, &used);
+  if (!xh) return LATER_ERR_WORKSPACE;
+  char* xl = o.prec == LATER_PREC_SPLIT3 ? xh + ldx * n * 2 : nullptr;
+  b.h += used;
+  b.hcap -= used;
+  return lln ? trsm_lln(b, m, n, A, lda, B, ldb, xh, xl, ldx) : trsm_rlt(b, m, n, A, lda, B, ldb, xh, xl, ldx);
+}
+
+later_status_t rtrmm(cudaStream_t st, int m, int n, const float* A, int64_t lda, const float* B, int64_t ldb,
+                     float* C, int64_t ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                     const Options& o) {
+  if (m < 0 || n < 0 || !A || !B || !C || lda < std::max(m, 1) || ldb < std::max(m, 1) || ldc < std::max(m, 1))
+    return LATER_ERR_INVALID_ARG;
+  if (m == 0 || n == 0) return LATER_OK;
+  if (!hwork || lhwork < rtrmm_hwork(m, n, o) || (reinterpret_cast<uintptr_t>(hwork) & 15)) return LATER_ERR_WORKSPACE;
+  B3 b = make_b3(st, o, work, lwork, hwork, lhwork);
+  Op16 bh;
+  size_t used = 0;
+  LATER_CHECK(copy16(b, m, n, B, ldb, &bh, &used));
+  b.h += used;
+  b.hcap -= used;
+  return trmm_rec(b, m, n, A, lda, B, ldb, bh, C, ldc);
+}
+
+later_status_t rpotrf(cudaStream_t st, char uplo, int n, float* A, int64_t lda, float* work, int64_t lwork,
+                      void* hwork, int64_t lhwork, const Options& o) {
+  if ((uplo | 0x20) != 'l') return LATER_ERR_NOT_SUPPORTED;
+  if (n < 0 || !A || lda < std::max(n, 1)) return LATER_ERR_INVALID_ARG;
+  if (n == 0) return LATER_OK;
+  if (n > NB && (!hwork || lhwork < rpotrf_hwork(n, o) || (reinterpret_cast<uintptr_t>(hwork) & 15)))
+    return LATER_ERR_WORKSPACE;
+  B3 b = make_b3(st, o, work, lwork, hwork, lhwork);
+  return potrf_rec(b, n, A, lda);
+}
+
+}  // namespace later

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/later_c.h"
+#include "blas3.cuh"
 #include "qr.cuh"
 #include "runtime.cuh"
 
@@ -79,6 +80,50 @@ later_status_t later_c_rhouqr(later_stream_t stream, int m, int n, float* A, int
 later_status_t later_c_ormqr(later_stream_t stream, int m, int n, float* W, int ldw, const float* Y, int ldy,
                              float* work, int64_t lwork) {
   return ormqr(reinterpret_cast<cudaStream_t>(stream), m, n, W, ldw, Y, ldy, work, lwork);
+}
+
+later_status_t later_c_blas3_bufsize(char op, char side, int m, int n, const later_options_t* opt, int64_t* lwork,
+                                     int64_t* lhwork) {
+  const Options o = options_from(opt);
+  if (m < 0 || n < 0) return LATER_ERR_INVALID_ARG;
+  int64_t h = 0;
+  switch (op | 0x20) {
+    case 's': h = rsyrk_hwork(m, n, o); break;
+    case 't': h = rtrsm_hwork(m, n, side, o); break;
+    case 'm': h = rtrmm_hwork(m, n, o); break;
+    case 'p': h = rpotrf_hwork(m, o); break;
+    default: return LATER_ERR_INVALID_ARG;
+  }
+  if (lwork) *lwork = splitk_work();
+  if (lhwork) *lhwork = h;
+  return LATER_OK;
+}
+
+later_status_t later_c_rsyrk(later_stream_t stream, int n, int k, float alpha, const float* A, int lda, float beta,
+                             float* C, int ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                             const later_options_t* opt) {
+  return rsyrk(reinterpret_cast<cudaStream_t>(stream), n, k, alpha, A, lda, beta, C, ldc, work, lwork, hwork, lhwork,
+               options_from(opt));
+}
+
+later_status_t later_c_rtrsm(later_stream_t stream, char uplo, char leri, char trans, int m, int n, const float* A,
+                             int lda, float* B, int ldb, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                             const later_options_t* opt) {
+  return rtrsm(reinterpret_cast<cudaStream_t>(stream), uplo, leri, trans, m, n, A, lda, B, ldb, work, lwork, hwork,
+               lhwork, options_from(opt));
+}
+
+later_status_t later_c_rtrmm(later_stream_t stream, int m, int n, const float* A, int lda, const float* B, int ldb,
+                             float* C, int ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                             const later_options_t* opt) {
+  return rtrmm(reinterpret_cast<cudaStream_t>(stream), m, n, A, lda, B, ldb, C, ldc, work, lwork, hwork, lhwork,
+               options_from(opt));
+}
+
+later_status_t later_c_rpotrf(later_stream_t stream, char uplo, int n, float* A, int lda, float* work,
+                              int64_t lwork, void* hwork, int64_t lhwork, const later_options_t* opt) {
+  return rpotrf(reinterpret_cast<cudaStream_t>(stream), uplo, n, A, lda, work, lwork, hwork, lhwork,
+                options_from(opt));
 }
 
 later_status_t later_c_gemm16(later_stream_t stream, char transa, char transb, int m, int n, int k, float alpha,

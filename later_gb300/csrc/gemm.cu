@@ -129,6 +129,8 @@ __global__ void __launch_bounds__(128, 1)
   const int kb0 = split * p.kb_per_split;
   const int kb1 = min(kb0 + p.kb_per_split, p.kb_total);
   const int nkb = kb1 - kb0;
+  // Lower-triangular output (SYRK): a tile entirely above the diagonal has no work.
+  if (p.lower && m0 + BM - 1 < n0 + p.diag) return;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -400,7 +402,7 @@ later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, lon
 
   // Split-K when the tile grid leaves SMs idle; at least 4 K blocks per split.
   int splits = 1;
-  if (tiles < nsm && s.partial && s.counters && tiles <= s.n_counters) {
+  if (tiles < nsm && s.partial) {
     int want = (nsm + tiles - 1) / tiles;
     int maxk = kb_total / 4;
     splits = want < maxk ? want : maxk;

@@ -300,14 +300,15 @@ __global__ void __launch_bounds__(256) tn_reduce_kernel(int nch, int ntiles, int
 // S staged in shared memory; each thread updates 4 rows x 4 columns. Optional
 // 16-bit copy of the updated Y (mode 0 fp16, 1 bf16, 2 split3 hi/lo).
 constexpr int NNR = 64;
-__global__ void __launch_bounds__(256) nn_update_kernel(int m, int k1, int k2, const float* __restrict__ X,
+__global__ void __launch_bounds__(256) nn_update_kernel(int m, int k1, int k2, float alpha, const float* __restrict__ X,
                                                         int64_t ldx, const float* __restrict__ S, int64_t lds,
-                                                        float* __restrict__ Y, int64_t ldy, void* yh, void* yl,
-                                                        int64_t ldh, int mode) {
+                                                        int s_trans, int lower, float* __restrict__ Y, int64_t ldy,
+                                                        void* yh, void* yl, int64_t ldh, int mode) {
   __shared__ float Ss[64][65];
   __shared__ float Xs[NNR][65];
   const int r0 = blockIdx.x * NNR;
   const int c0 = blockIdx.y * 64;
+  if (lower && r0 + NNR - 1 < c0) return;  // tile entirely above the diagonal
   const int mm = min(NNR, m - r0);
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // rows tx + 16 a, cols ty + 16 b
   float y[4][4];
@@ -324,7 +325,10 @@ __global__ void __launch_bounds__(256) nn_update_kernel(int m, int k1, int k2, c
     for (int u = 0; u < 16; ++u) {
       const int e = threadIdx.x + 256 * u;
       const int i = e % 64, j = e / 64;
-      sv[u] = (k0 + i < k1 && c0 + j < k2) ? S[k0 + i + static_cast<int64_t>(c0 + j) * lds] : 0.f;
+      const bool ins = (k0 + i < k1 && c0 + j < k2);
+      sv[u] = !ins ? 0.f
+                   : (s_trans ? S[c0 + j + static_cast<int64_t>(k0 + i) * lds]
+                              : S[k0 + i + static_cast<int64_t>(c0 + j) * lds]);
       xv[u] = (i < mm && k0 + j < k1) ? __ldcg(&X[r0 + i + static_cast<int64_t>(k0 + j) * ldx]) : 0.f;
     }
     __syncthreads();
@@ -346,7 +350,7 @@ __global__ void __launch_bounds__(256) nn_update_kernel(int m, int k1, int k2, c
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) y[u][v] -= xr[u] * sr[v];
+        for (int v = 0; v < 4; ++v) y[u][v] += alpha * (xr[u] * sr[v]);
     }
   }
 #pragma unroll
@@ -354,7 +358,7 @@ __global__ void __launch_bounds__(256) nn_update_kernel(int m, int k1, int k2, c
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const int i = tx + 16 * u, j = c0 + ty + 16 * v;
-      if (i < mm && j < k2) {
+      if (i < mm && j < k2 && (!lower || r0 + i >= j)) {
         const float val = y[u][v];
         Y[r0 + i + static_cast<int64_t>(j) * ldy] = val;
         if (yh) {
@@ -468,16 +472,22 @@ later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, in
   return LATER_OK;
 }
 
-later_status_t simt_nn_sub(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* S,
-                           int64_t lds, float* Y, int64_t ldy, void* yh, void* yl, int64_t ldh, int out_prec) {
+later_status_t simt_gemm_acc(cudaStream_t s, int m, int k1, int k2, float alpha, const float* X, int64_t ldx,
+                             const float* S, int64_t lds, int s_trans, int lower, float* Y, int64_t ldy, void* yh,
+                             void* yl, int64_t ldh, int out_prec) {
   if (m <= 0 || k1 <= 0 || k2 <= 0) return LATER_OK;
   if ((k2 + 63) / 64 > 65535) return LATER_ERR_NOT_SUPPORTED;
   const int mode = out_prec == LATER_PREC_BF16 ? 1 : (out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
   TraceScope trace(s, TRACE_LEAF_GEMM, 2.0 * m * k1 * k2);
-  nn_update_kernel<<<dim3((m + NNR - 1) / NNR, (k2 + 63) / 64), 256, 0, s>>>(m, k1, k2, X, ldx, S, lds, Y, ldy, yh,
-                                                                             yl, ldh, mode);
+  nn_update_kernel<<<dim3((m + NNR - 1) / NNR, (k2 + 63) / 64), 256, 0, s>>>(m, k1, k2, alpha, X, ldx, S, lds, s_trans,
+                                                                             lower, Y, ldy, yh, yl, ldh, mode);
   note_launch();
   return cuda_status(cudaGetLastError());
+}
+
+later_status_t simt_nn_sub(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* S,
+                           int64_t lds, float* Y, int64_t ldy, void* yh, void* yl, int64_t ldh, int out_prec) {
+  return simt_gemm_acc(s, m, k1, k2, -1.f, X, ldx, S, lds, 0, 0, Y, ldy, yh, yl, ldh, out_prec);
 }
 
 }  // namespace later

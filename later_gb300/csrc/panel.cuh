@@ -44,4 +44,10 @@ later_status_t simt_nn_sub(cudaStream_t s, int m, int k1, int k2, const float* X
                            int64_t lds, float* Y, int64_t ldy, void* yh = nullptr, void* yl = nullptr,
                            int64_t ldh = 0, int out_prec = LATER_PREC_FP16);
 
+// Y += alpha X op(S), op(S) = S (k1 x k2) or, with s_trans, the transpose of a
+// stored k2 x k1 S; with `lower`, only Y[i][j], i >= j, is updated. FP32 SIMT.
+later_status_t simt_gemm_acc(cudaStream_t s, int m, int k1, int k2, float alpha, const float* X, int64_t ldx,
+                             const float* S, int64_t lds, int s_trans, int lower, float* Y, int64_t ldy,
+                             void* yh = nullptr, void* yl = nullptr, int64_t ldh = 0, int out_prec = 0);
+
 }  // namespace later

@@ -236,3 +236,98 @@ def ormqr(W: np.ndarray, Y: np.ndarray) -> np.ndarray:
     m, n = W.shape
     y1 = np.tril(np.asarray(Y, dtype=F32)[:n, :n], -1) + np.eye(n, dtype=F32)
     return (np.eye(m, n, dtype=F32) - W.astype(F32) @ y1.T).astype(F32)
+
+
+# --------------------------------------------------------- BLAS-3 / Cholesky
+def _solve_tri(L, B, lower=True, trans=False, side="left"):
+    import scipy.linalg as sl
+    L = np.asarray(L, dtype=F32)
+    B = np.asarray(B, dtype=F32)
+    if side == "left":
+        return sl.solve_triangular(L, B, lower=lower, trans=1 if trans else 0).astype(F32)
+    # X op(L) = B  <=>  op(L)^T X^T = B^T
+    return sl.solve_triangular(L, B.T, lower=lower, trans=0 if trans else 1).T.astype(F32)
+
+
+def rsyrk(alpha, A, beta, C, prec="fp16"):
+    """C <- alpha A A^T + beta C, lower triangle — syrk, BLAS/later_rsyrk.cu:12-77
+    (every block is a GemmEx of FP16-rounded A with FP32 accumulation)."""
+    a = round16(np.asarray(A, dtype=F32), prec)
+    out = np.array(C, dtype=F32)
+    full = (F32(alpha) * (a @ a.T) + F32(beta) * out).astype(F32)
+    il = np.tril_indices(out.shape[0])
+    out[il] = full[il]
+    return out
+
+
+def rtrsm(side, L, B, prec="fp16", leaf=256):
+    """Recursive TRSM with a lower L — trsm_l_l_n / trsm_l_r_t, BLAS/later_rtrsm.cu:75-163.
+    side 'l': L X = B (split on rows); side 'r': X L^T = B (split on columns).
+    Leaf (<= leaf): FP32 substitution (cublasStrsm); updates: FP16 GemmEx."""
+    L = np.asarray(L, dtype=F32)
+    X = np.array(B, dtype=F32)
+
+    def rec_l(L, X):
+        m = L.shape[0]
+        if m <= leaf:
+            X[:] = _solve_tri(L, X, lower=True, side="left")
+            return
+        h = m // 2
+        rec_l(L[:h, :h], X[:h])
+        X[h:] -= tc_gemm(L[h:, :h], X[:h], prec)
+        rec_l(L[h:, h:], X[h:])
+
+    def rec_r(L, X):
+        n = L.shape[0]
+        if n <= leaf:
+            X[:] = _solve_tri(L, X, lower=True, trans=True, side="right")
+            return
+        h = n // 2
+        rec_r(L[:h, :h], X[:, :h])
+        X[:, h:] -= tc_gemm(X[:, :h], L[h:, :h].T, prec)
+        rec_r(L[h:, h:], X[:, h:])
+
+    (rec_l if side == "l" else rec_r)(L, X)
+    return X
+
+
+def rtrmm(L, B, prec="fp16", leaf=256):
+    """C = L B, L lower — trmm, BLAS/later_rtrmm.cu:14-71 (leaf cublasStrmm in FP32,
+    off-diagonal GemmEx into tempC, then C2 += tempC)."""
+    L = np.asarray(L, dtype=F32)
+    B = np.asarray(B, dtype=F32)
+    C = np.zeros_like(B)
+
+    def rec(L, B, C):
+        m = L.shape[0]
+        if m <= leaf:
+            C[:] = (np.tril(L) @ B).astype(F32)
+            return
+        h = m // 2
+        rec(L[:h, :h], B[:h], C[:h])
+        tmp = tc_gemm(L[h:, :h], B[:h], prec)
+        rec(L[h:, h:], B[h:], C[h:])
+        C[h:] += tmp
+
+    rec(L, B, C)
+    return C
+
+
+def rpotrf(A, prec="fp16", leaf=2048):
+    """Recursive lower Cholesky — l_potrf, Cholesky/later_rpotrf.cu:22-66: leaf spotrf
+    (<= 2048), off-diagonal later_rtrsm('l','r','t'), trailing later_rsyrk(-1, 1)."""
+    a = np.array(A, dtype=F32)
+
+    def rec(a):
+        n = a.shape[0]
+        if n <= leaf:
+            a[:] = np.linalg.cholesky(a.astype(F32)).astype(F32)
+            return
+        h = n // 2
+        rec(a[:h, :h])
+        a[h:, :h] = rtrsm("r", a[:h, :h], a[h:, :h], prec)
+        a[h:, h:] = rsyrk(-1.0, a[h:, :h], 1.0, a[h:, h:], prec)
+        rec(a[h:, h:])
+
+    rec(a)
+    return np.tril(a)
