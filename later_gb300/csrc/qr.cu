@@ -195,7 +195,7 @@ QrNeed rgsqrf_need(int m, int n, const Options& o) {
   q.min_work = fixed + std::max<int64_t>(stack, 4096 + 128);
   q.rec_work = fixed + std::max(std::max(stack, leaf_parts), splitk);
   const int64_t ldh = round_up(m, 8);
-  q.hwork = ldh * n * (o.prec == LATER_PREC_SPLIT3 ? 2 : 1) + 64;
+  q.hwork = ldh * n * (o.prec == LATER_PREC_SPLIT3 ? 2 : 1);
   return q;
 }
 
@@ -398,7 +398,7 @@ QrNeed rhouqr_need(int m, int n, const Options& o) {
   const int64_t splitk = static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 128;
   q.min_work = fixed + std::max<int64_t>(stack, 4 * 4096 + 128);
   q.rec_work = fixed + std::max(std::max(stack, parts), splitk);
-  q.hwork = round_up(m, 8) * n * (o.prec == LATER_PREC_SPLIT3 ? 2 : 1) + 64;
+  q.hwork = round_up(m, 8) * n * (o.prec == LATER_PREC_SPLIT3 ? 2 : 1);
   return q;
 }
 
