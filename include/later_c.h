@@ -171,6 +171,24 @@ later_status_t later_c_gemm16(later_stream_t stream, char transa, char transb, i
                               int64_t lwork);
 
 /*
+ * later_c_gemm16 without a caller workspace (no counterpart in the reference).
+ * For callers that cannot allocate device memory (a host framework whose own
+ * pool owns all device memory and forbids plug-ins from calling the
+ * allocator, or a latency-critical path that cannot afford cudaMalloc's
+ * implicit synchronisation): the split-K scratch is a fixed device array of
+ * LATER_NOALLOC_SCRATCH_FLOATS floats (16 MiB) inside this library, held by
+ * every GPU that loads it until exit. The call allocates nothing. The first
+ * call on a device looks up the array's address; make it before any stream
+ * capture. Requests whose output, rounded up to 128 x 256 tiles, exceeds the
+ * array return LATER_ERR_WORKSPACE (use later_c_gemm16 for those). All calls
+ * share the array: calls whose kernels overlap on the GPU race on it.
+ */
+#define LATER_NOALLOC_SCRATCH_FLOATS 4194304
+later_status_t later_c_gemm16_noalloc(later_stream_t stream, char transa, char transb, int m, int n, int k,
+                                      float alpha, const void* A, int lda, const void* B, int ldb, float beta,
+                                      const float* C, int ldc, float* D, int ldd, int precision);
+
+/*
  * FP32 -> 16-bit conversion of an m x n column-major block (the role of
  * util/util.cu:24-32 s2h). precision FP16 / BF16 writes `hi`; SPLIT3 writes
  * hi = fp16(x) and lo = fp16((x - hi) * 2048).
