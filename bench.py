@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--cpu-m", type=int, default=16384, help="CPU sample rows")
     p.add_argument("--cpu-n", type=int, default=1024, help="CPU sample columns")
+    p.add_argument("--gemm", type=int, nargs=3, metavar=("M", "N", "K"), default=None,
+                   help="time only the tensor-core GEMM R12 = Q1^T A2 of this shape (TN, FP16) — the "
+                        "top-level trailing-update product of rgsqrf; used for kernel profiling")
     return p.parse_args()
 
 
@@ -284,9 +287,16 @@ def run_ours(a, rank, world, local_rank):
     peak = peak or 1900.0
     top_ach = tr["top_gemm_flops"] / tr["top_gemm_ms"] / 1e9 if tr["top_gemm_ms"] else None
     all_ach = tr["gemm_flops"] / tr["gemm_ms"] / 1e9 if tr["gemm_ms"] else None
+    traffic = None
+    prof = ROOT / "profiles" / f"tc_gemm_tn_{m // 2}x{n - n // 2}x{m}.md"
+    if prof.exists():  # DRAM bytes of the same launch from the committed ncu capture
+        for line in prof.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = int(line.split(":")[1])
     roof = {"bound": "tensor", "kernel": "tc_gemm_kernel (largest launch: top-level trailing update)",
             "achieved": top_ach, "peak": peak, "unit": "TFLOP/s", "frac": (top_ach / peak) if top_ach else None,
-            "peak_source": peak_src, "traffic": None,
+            "peak_source": peak_src, "traffic": traffic,
+            "traffic_source": str(prof.relative_to(ROOT)) if traffic else None,
             "all_gemm_achieved": all_ach, "all_gemm_frac": (all_ach / peak) if all_ach else None}
 
     cpu = None
@@ -314,8 +324,37 @@ def run_ours(a, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def run_gemm_only(a):
+    """One TN GEMM shape, FP16 operands, FP32 output, through later_c_gemm16."""
+    import torch
+    import later_gb300 as lg
+    M, N, K = a.gemm
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    A = lg.empty_colmajor(K, M, dtype=torch.float16)
+    A.copy_(torch.randn(K, M, generator=g, device="cuda"))
+    B = lg.empty_colmajor(K, N, dtype=torch.float16)
+    B.copy_(torch.randn(K, N, generator=g, device="cuda"))
+    D = lg.empty_colmajor(M, N)
+    work = torch.empty(1 << 24, dtype=torch.float32, device="cuda")
+    for _ in range(a.warmup):
+        lg.gemm16("T", "N", A, B, D=D, work=work)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.steps):
+        lg.gemm16("T", "N", A, B, D=D, work=work)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    print(json.dumps({"metric": "tensor-core GEMM TFLOP/s (2MNK)", "value": 2.0 * M * N * K / ms / 1e9,
+                      "unit": "TFLOP/s", "ms_per_step": ms, "shape": [M, N, K], "op": "TN fp16->fp32"}), flush=True)
+
+
 def main():
     a = parse()
+    if a.gemm:
+        run_gemm_only(a)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
