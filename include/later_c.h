@@ -154,6 +154,79 @@ later_status_t later_c_rtrmm(later_stream_t stream, int m, int n, const float* A
 later_status_t later_c_rpotrf(later_stream_t stream, char uplo, int n, float* A, int lda, float* work,
                               int64_t lwork, void* hwork, int64_t lhwork, const later_options_t* opt);
 
+/* ----------------------------------------------- mixed-precision solvers */
+/* No counterpart in the reference (LATER has the factorisations only). Both
+ * solvers synchronise `stream` (host convergence test between iterations);
+ * nrhs <= 16; X is FP64 (n x nrhs, ldx). FP64 arithmetic runs only in the
+ * residual r = B - A X, A^T r and the update of X. */
+
+typedef struct {
+  int iterations;          /* refinement steps taken */
+  int factor_precision;    /* later_precision_t the factorisation finally used */
+  double backward_error;   /* final normwise backward error, computed in FP64 */
+} later_solve_info_t;
+
+later_status_t later_c_spd_solve_bufsize(int n, int nrhs, const later_options_t* opt, int64_t* lwork,
+                                         int64_t* lhwork);
+
+/*
+ * SPD solve A X = B: rpotrf (opt->precision; a non-SPD 16-bit factorisation
+ * is redone in SPLIT3), FP32 triangular solves, then FP64 iterative
+ * refinement until max_c ||r_c||inf / (||A||inf ||x_c||inf + ||b_c||inf) <= tol
+ * or max_iter steps. A (n x n FP32) and B are not modified.
+ */
+later_status_t later_c_spd_solve(later_stream_t stream, int n, int nrhs, const float* A, int lda, const float* B,
+                                 int ldb, double* X, int ldx, float* work, int64_t lwork, void* hwork,
+                                 int64_t lhwork, const later_options_t* opt, int max_iter, double tol,
+                                 later_solve_info_t* info);
+
+later_status_t later_c_ls_solve_bufsize(int m, int n, int nrhs, const later_options_t* opt, int64_t* lwork,
+                                        int64_t* lhwork);
+
+/*
+ * Least squares min ||A X - B|| (m >= n, n a multiple of 32): rgsqrf
+ * (opt->precision; SPLIT3 recommended for kappa > 1e3), X = R^-1 Q^T B, then
+ * X += R^-1 Q^T (B - A X) with FP64 residuals until the backward error of the
+ * augmented system, max_c ||A^T r_c||inf / (||A_aug||inf max(||r_c||inf, ||x_c||inf)
+ * + ||b_c||inf), is <= tol or max_iter steps. A and B are not modified.
+ */
+later_status_t later_c_ls_solve(later_stream_t stream, int m, int n, int nrhs, const float* A, int lda,
+                                const float* B, int ldb, double* X, int ldx, float* work, int64_t lwork,
+                                void* hwork, int64_t lhwork, const later_options_t* opt, int max_iter, double tol,
+                                later_solve_info_t* info);
+
+/* ---------------------------------------------------------- batched QR */
+/* No counterpart in the reference. Many independent FP32 matrices of uneven
+ * sizes (m >= n, n <= 256) factored A_i = Q_i R_i in one persistent-kernel
+ * launch: Q_i overwrites A_i, R_i (n x n) gets the upper factor with a
+ * positive diagonal and zeros below it. */
+
+typedef struct {
+  float* A;     /* device, column-major m x n */
+  float* R;     /* device, n x n */
+  int64_t lda;
+  int64_t ldr;
+  int m;
+  int n;
+} later_qr_item_t;
+
+/* Device bytes of the plan for `count` matrices. */
+int64_t later_c_batched_plan_bytes(int count);
+
+/* Sorts the matrices by decreasing cost (2 n^2 m) and uploads their
+ * descriptors into `plan` (device). Synchronises `stream`. */
+later_status_t later_c_batched_qr_plan(later_stream_t stream, int count, const later_qr_item_t* items, void* plan,
+                                       int64_t plan_bytes);
+
+/* Factors every matrix of the plan: one counter reset (`queue`, one device
+ * int) and one launch, so it can be captured in a CUDA graph. `status`
+ * (device, count ints, may be NULL) receives 0 or LATER_ERR_NUMERIC per
+ * matrix (a 32-column panel whose Cholesky QR broke down: kappa too large
+ * for CholQR2 in FP32). `variant` picks the tile shape (0 .. 3, see
+ * later_gb300.autotune); -1 uses variant 0. */
+later_status_t later_c_batched_qr_run(later_stream_t stream, int count, const void* plan, int* queue, int* status,
+                                      int variant);
+
 /* --------------------------------------------------------- building blocks */
 
 /*

@@ -20,7 +20,8 @@ from . import build as _build
 __all__ = [
     "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
     "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "later_rsyrk", "later_rtrsm",
-    "later_rtrmm", "later_rpotrf", "blas3_bufsize", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
+    "later_rtrmm", "later_rpotrf", "blas3_bufsize",
+    "spd_solve", "ls_solve", "BatchedQR", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
     "trace_end",
 ]
 
@@ -67,10 +68,25 @@ _SIGS = {
                            _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_rtrmm": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_rpotrf": (_i, [_vp, ctypes.c_char, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
+    "later_c_spd_solve_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "later_c_ls_solve_bufsize": (_i, [_i, _i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64),
+                                      ctypes.POINTER(_i64)]),
+    "later_c_batched_plan_bytes": (_i64, [_i]),
+    "later_c_batched_qr_plan": (_i, [_vp, _i, _vp, _vp, _i64]),
+    "later_c_batched_qr_run": (_i, [_vp, _i, _vp, _vp, _vp, _i]),
     "later_c_launch_count": (ctypes.c_uint64, []),
     "later_c_trace_begin": (None, []),
     "later_c_trace_end": (_i, [_vp]),
 }
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("factor_precision", ctypes.c_int), ("backward_error", ctypes.c_double)]
+
+
+class QrItem(ctypes.Structure):
+    _fields_ = [("A", ctypes.c_void_p), ("R", ctypes.c_void_p), ("lda", ctypes.c_int64), ("ldr", ctypes.c_int64),
+                ("m", ctypes.c_int), ("n", ctypes.c_int)]
 
 
 class Trace(ctypes.Structure):
@@ -285,6 +301,93 @@ def later_rpotrf(uplo, n, A, *, precision="fp16", work=None, hwork=None, stream=
     _check(lib().later_c_rpotrf(_stream(stream), uplo.encode(), n, A.data_ptr(), _ld(A, "A"), work.data_ptr(),
                                 work.numel(), hwork.data_ptr(), hwork.numel(), ctypes.byref(o)), "later_rpotrf")
     return A
+
+
+def _solve_ws(lw, lh, device, work, hwork):
+    import torch
+    if work is None:
+        work = torch.empty(lw, dtype=torch.float32, device=device)
+    if hwork is None:
+        hwork = torch.empty(max(lh, 8), dtype=torch.float16, device=device)
+    return work, hwork
+
+
+def _bind_solver(name):
+    fn = getattr(lib(), name)
+    fn.restype = _i
+    if name == "later_c_spd_solve":
+        fn.argtypes = [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options), _i,
+                       ctypes.c_double, ctypes.POINTER(SolveInfo)]
+    else:
+        fn.argtypes = [_vp, _i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options), _i,
+                       ctypes.c_double, ctypes.POINTER(SolveInfo)]
+    return fn
+
+
+def spd_solve(A, B, *, precision="fp16", max_iter=30, tol=1e-12, work=None, hwork=None, stream=None):
+    """SPD solve with FP64 refinement; returns (X (FP64, column-major), info dict)."""
+    import torch
+    n, k = B.shape
+    o = Options.make(precision)
+    lw, lh = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().later_c_spd_solve_bufsize(n, k, ctypes.byref(o), ctypes.byref(lw), ctypes.byref(lh)), "bufsize")
+    work, hwork = _solve_ws(lw.value, lh.value, A.device, work, hwork)
+    X = empty_colmajor(n, k, dtype=torch.float64, device=A.device)
+    info = SolveInfo()
+    _check(_bind_solver("later_c_spd_solve")(_stream(stream), n, k, A.data_ptr(), _ld(A, "A"), B.data_ptr(),
+                                             _ld(B, "B"), X.data_ptr(), _ld(X, "X"), work.data_ptr(), work.numel(),
+                                             hwork.data_ptr(), hwork.numel(), ctypes.byref(o), max_iter, tol,
+                                             ctypes.byref(info)), "later_c_spd_solve")
+    return X, {"iterations": info.iterations, "backward_error": info.backward_error,
+               "factor_precision": info.factor_precision}
+
+
+def ls_solve(A, B, *, precision="split3", max_iter=30, tol=1e-6, work=None, hwork=None, stream=None):
+    """Least-squares solve with FP64-residual refinement; returns (X (FP64), info dict)."""
+    import torch
+    m, n = A.shape
+    k = B.shape[1]
+    o = Options.make(precision)
+    lw, lh = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().later_c_ls_solve_bufsize(m, n, k, ctypes.byref(o), ctypes.byref(lw), ctypes.byref(lh)), "bufsize")
+    work, hwork = _solve_ws(lw.value, lh.value, A.device, work, hwork)
+    X = empty_colmajor(n, k, dtype=torch.float64, device=A.device)
+    info = SolveInfo()
+    _check(_bind_solver("later_c_ls_solve")(_stream(stream), m, n, k, A.data_ptr(), _ld(A, "A"), B.data_ptr(),
+                                            _ld(B, "B"), X.data_ptr(), _ld(X, "X"), work.data_ptr(), work.numel(),
+                                            hwork.data_ptr(), hwork.numel(), ctypes.byref(o), max_iter, tol,
+                                            ctypes.byref(info)), "later_c_ls_solve")
+    return X, {"iterations": info.iterations, "backward_error": info.backward_error,
+               "factor_precision": info.factor_precision}
+
+
+class BatchedQR:
+    """Plan once, run many times (the run is one launch and can be captured in a CUDA graph).
+
+    `mats` are column-major FP32 CUDA tensors (m_i x n_i, m_i >= n_i, n_i <= 256); Q_i overwrites them and
+    R_i (n_i x n_i) is written into `rs` (allocated when not given).
+    """
+
+    def __init__(self, mats, rs=None, stream=None):
+        import torch
+        self.mats = list(mats)
+        dev = self.mats[0].device
+        self.rs = rs if rs is not None else [empty_colmajor(a.shape[1], a.shape[1], device=dev) for a in self.mats]
+        items = (QrItem * len(self.mats))()
+        for i, (a, r) in enumerate(zip(self.mats, self.rs)):
+            items[i] = QrItem(a.data_ptr(), r.data_ptr(), _ld(a, "A"), _ld(r, "R"), a.shape[0], a.shape[1])
+        nb = int(lib().later_c_batched_plan_bytes(len(self.mats)))
+        self.plan = torch.empty(nb, dtype=torch.uint8, device=dev)
+        self.queue = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(len(self.mats), dtype=torch.int32, device=dev)
+        _check(lib().later_c_batched_qr_plan(_stream(stream), len(self.mats), ctypes.cast(items, ctypes.c_void_p),
+                                             self.plan.data_ptr(), nb), "batched_qr_plan")
+
+    def run(self, variant=-1, stream=None):
+        _check(lib().later_c_batched_qr_run(_stream(stream), len(self.mats), self.plan.data_ptr(),
+                                            self.queue.data_ptr(), self.status.data_ptr(), int(variant)),
+               "batched_qr_run")
+        return self.rs
 
 
 def gemm16(transa, transb, A, B, alpha=1.0, beta=0.0, C=None, D=None, precision="fp16", work=None, stream=None):

@@ -115,6 +115,35 @@ __global__ void __launch_bounds__(32) trsm_lln_leaf(int nb, int n, const float* 
   }
 }
 
+// L^T X = B (left, lower, transposed), L nb x nb (nb <= 128), B nb x n:
+// backward substitution, one thread per column of B staged in shared memory.
+__global__ void __launch_bounds__(32) trsm_llt_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl, float* B,
+                                                    int64_t ldb) {
+  extern __shared__ float sm[];
+  float* Ls = sm;             // [k][i] at k*129 + i  (= L[k][i])
+  float* Bs = sm + NB * 129;  // [col][row]
+  const int c0 = blockIdx.x * 32;
+  for (int e = threadIdx.x; e < nb * nb; e += 32) {
+    const int k = e % nb, i = e / nb;
+    Ls[k * 129 + i] = (k >= i) ? L[k + static_cast<int64_t>(i) * ldl] : 0.f;
+  }
+  for (int c = 0; c < 32; ++c)
+    for (int r = threadIdx.x; r < nb; r += 32)
+      Bs[c * 129 + r] = (c0 + c < n) ? B[r + static_cast<int64_t>(c0 + c) * ldb] : 0.f;
+  __syncthreads();
+  float* x = Bs + threadIdx.x * 129;
+  for (int i = nb - 1; i >= 0; --i) {
+    float acc = x[i];
+    for (int k = i + 1; k < nb; ++k) acc -= Ls[k * 129 + i] * x[k];
+    x[i] = acc / Ls[i * 129 + i];
+  }
+  __syncthreads();
+  for (int c = 0; c < 32; ++c) {
+    if (c0 + c >= n) break;
+    for (int r = threadIdx.x; r < nb; r += 32) B[r + static_cast<int64_t>(c0 + c) * ldb] = Bs[c * 129 + r];
+  }
+}
+
 // C = L B (left, lower), L nb x nb (nb <= 128), B nb x n, C nb x n. One CTA
 // per 64 columns; each thread accumulates 8 rows x 4 columns... of its share.
 __global__ void __launch_bounds__(256) trmm_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl,
@@ -208,6 +237,7 @@ bool smem_attr(const void* fn, size_t bytes) {
 struct B3 {
   cudaStream_t st;
   Options o;
+  Arena* ws = nullptr;  // FP32 scratch for SIMT partial products (optional)
   char* h;      // 16-bit scratch (hwork) cursor
   size_t hcap;  // bytes
   Scratch sc;   // split-K scratch
@@ -324,6 +354,39 @@ later_status_t trsm_lln(B3& b, int m, int n, const float* L, int64_t ldl, float*
                   xl ? xl + m1 * 2 : nullptr, ldh, fp32_lim);
 }
 
+// L^T X = B, L m x m lower, B m x n (in place). The update B1 -= L21^T X2 runs
+// in FP32 below fp32_lim, else on the tensor cores (16-bit copies converted).
+later_status_t trsm_llt(B3& b, int m, int n, const float* L, int64_t ldl, float* B, int64_t ldb,
+                        int fp32_lim = kFp32Trsm) {
+  if (m <= NB) {
+    const size_t smem = (NB * 129 + 32 * 129) * sizeof(float);
+    if (!smem_attr(reinterpret_cast<const void*>(trsm_llt_leaf), smem)) return LATER_ERR_CUDA;
+    TraceScope tr(b.st, TRACE_OTHER);
+    trsm_llt_leaf<<<(n + 31) / 32, 32, smem, b.st>>>(m, n, L, ldl, B, ldb);
+    note_launch();
+    return cuda_status(cudaGetLastError());
+  }
+  const int m1 = half64(m), m2 = m - m1;
+  LATER_CHECK(trsm_llt(b, m2, n, L + m1 + m1 * ldl, ldl, B + m1, ldb, fp32_lim));
+  // B1 -= L21^T X2   (L21 = L[m1:, :m1], m2 x m1; X2 = B[m1:], m2 x n)
+  if (m <= fp32_lim) {
+    if (b.ws == nullptr) return LATER_ERR_WORKSPACE;
+    LATER_CHECK(simt_tn(b.st, m2, m1, n, L + m1, ldl, B + m1, ldb, B, ldb, 1, *b.ws, -1.f));
+  } else {
+    B3 sub = b;
+    Op16 l21, x2;
+    size_t u1 = 0, u2 = 0;
+    LATER_CHECK(copy16(sub, m2, m1, L + m1, ldl, &l21, &u1));
+    sub.h += u1;
+    sub.hcap -= u1;
+    LATER_CHECK(copy16(sub, m2, n, B + m1, ldb, &x2, &u2));
+    sub.h += u2;
+    sub.hcap -= u2;
+    LATER_CHECK(gemm(sub, 'T', 'N', m1, n, m2, -1.f, l21, x2, 1.f, B, ldb));
+  }
+  return trsm_llt(b, m1, n, L, ldl, B, ldb, fp32_lim);
+}
+
 // C = L B, L m x m lower, B m x n (its 16-bit copy bh, ldbh), C m x n.
 later_status_t trmm_rec(B3& b, int m, int n, const float* L, int64_t ldl, const float* B, int64_t ldb, const Op16& bh,
                         float* C, int64_t ldc) {
@@ -437,16 +500,28 @@ later_status_t rsyrk(cudaStream_t st, int n, int k, float alpha, const float* A,
 later_status_t rtrsm(cudaStream_t st, char uplo, char leri, char trans, int m, int n, const float* A, int64_t lda,
                      float* B, int64_t ldb, float* work, int64_t lwork, void* hwork, int64_t lhwork,
                      const Options& o) {
+  return rtrsm_lim(st, uplo, leri, trans, m, n, A, lda, B, ldb, work, lwork, hwork, lhwork, o, kFp32Trsm);
+}
+
+later_status_t rtrsm_lim(cudaStream_t st, char uplo, char leri, char trans, int m, int n, const float* A,
+                         int64_t lda, float* B, int64_t ldb, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                         const Options& o, int fp32_lim) {
   auto lc = [](char c) { return static_cast<char>(c | 0x20); };
   const char u = lc(uplo), s = lc(leri), t = lc(trans);
   const bool lln = (u == 'l' && s == 'l' && t == 'n');
   const bool lrt = (u == 'l' && s == 'r' && t == 't');
-  if (!lln && !lrt) return LATER_ERR_NOT_SUPPORTED;
-  if (m < 0 || n < 0 || !A || !B || ldb < std::max(m, 1) || lda < std::max(lln ? m : n, 1)) return LATER_ERR_INVALID_ARG;
+  const bool llt = (u == 'l' && s == 'l' && t == 't');  // extension: L^T X = B
+  if (!lln && !lrt && !llt) return LATER_ERR_NOT_SUPPORTED;
+  if (m < 0 || n < 0 || !A || !B || ldb < std::max(m, 1) || lda < std::max(lrt ? n : m, 1)) return LATER_ERR_INVALID_ARG;
   if (m == 0 || n == 0) return LATER_OK;
   if (!hwork || lhwork < rtrsm_hwork(m, n, s, o) || (reinterpret_cast<uintptr_t>(hwork) & 15))
     return LATER_ERR_WORKSPACE;
   B3 b = make_b3(st, o, work, lwork, hwork, lhwork);
+  if (llt) {
+    Arena ws(work, work ? static_cast<size_t>(std::max<int64_t>(lwork, 0)) * sizeof(float) : 0);
+    b.ws = work ? &ws : nullptr;
+    return trsm_llt(b, m, n, A, lda, B, ldb, fp32_lim);
+  }
   const int64_t ldx = round_up(m, 8);
   size_t used = 0;
   char* xh = take16(b, ldx * n, &used);
@@ -454,7 +529,8 @@ later_status_t rtrsm(cudaStream_t st, char uplo, char leri, char trans, int m, i
   char* xl = o.prec == LATER_PREC_SPLIT3 ? xh + ldx * n * 2 : nullptr;
   b.h += used;
   b.hcap -= used;
-  return lln ? trsm_lln(b, m, n, A, lda, B, ldb, xh, xl, ldx) : trsm_rlt(b, m, n, A, lda, B, ldb, xh, xl, ldx);
+  return lln ? trsm_lln(b, m, n, A, lda, B, ldb, xh, xl, ldx, fp32_lim)
+             : trsm_rlt(b, m, n, A, lda, B, ldb, xh, xl, ldx, fp32_lim);
 }
 
 later_status_t rtrmm(cudaStream_t st, int m, int n, const float* A, int64_t lda, const float* B, int64_t ldb,

@@ -19,6 +19,11 @@ later_status_t rsyrk(cudaStream_t st, int n, int k, float alpha, const float* A,
                      int64_t ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
 later_status_t rtrsm(cudaStream_t st, char uplo, char leri, char trans, int m, int n, const float* A, int64_t lda,
                      float* B, int64_t ldb, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
+// rtrsm with the FP32 / tensor-core switch at `fp32_lim` (rtrsm uses the
+// reference's 256; the solvers pass INT_MAX: all-FP32 updates).
+later_status_t rtrsm_lim(cudaStream_t st, char uplo, char leri, char trans, int m, int n, const float* A,
+                         int64_t lda, float* B, int64_t ldb, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                         const Options& o, int fp32_lim);
 later_status_t rtrmm(cudaStream_t st, int m, int n, const float* A, int64_t lda, const float* B, int64_t ldb,
                      float* C, int64_t ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork,
                      const Options& o);

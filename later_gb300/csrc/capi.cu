@@ -6,6 +6,7 @@
 #include "blas3.cuh"
 #include "qr.cuh"
 #include "runtime.cuh"
+#include "solve.cuh"
 
 using namespace later;
 
@@ -124,6 +125,78 @@ later_status_t later_c_rpotrf(later_stream_t stream, char uplo, int n, float* A,
                               int64_t lwork, void* hwork, int64_t lhwork, const later_options_t* opt) {
   return rpotrf(reinterpret_cast<cudaStream_t>(stream), uplo, n, A, lda, work, lwork, hwork, lhwork,
                 options_from(opt));
+}
+
+later_status_t later_c_spd_solve_bufsize(int n, int nrhs, const later_options_t* opt, int64_t* lwork,
+                                         int64_t* lhwork) {
+  if (n < 1 || nrhs < 1) return LATER_ERR_INVALID_ARG;
+  const SolveNeed s = spd_solve_need(n, nrhs, options_from(opt));
+  if (lwork) *lwork = s.work;
+  if (lhwork) *lhwork = s.hwork;
+  return LATER_OK;
+}
+
+later_status_t later_c_spd_solve(later_stream_t stream, int n, int nrhs, const float* A, int lda, const float* B,
+                                 int ldb, double* X, int ldx, float* work, int64_t lwork, void* hwork,
+                                 int64_t lhwork, const later_options_t* opt, int max_iter, double tol,
+                                 later_solve_info_t* info) {
+  SolveInfo si;
+  const later_status_t s = spd_solve(reinterpret_cast<cudaStream_t>(stream), n, nrhs, A, lda, B, ldb, X, ldx, work,
+                                     lwork, hwork, lhwork, options_from(opt), max_iter, tol, &si);
+  if (info) {
+    info->iterations = si.iterations;
+    info->factor_precision = si.factor_precision;
+    info->backward_error = si.backward_error;
+  }
+  return s;
+}
+
+later_status_t later_c_ls_solve_bufsize(int m, int n, int nrhs, const later_options_t* opt, int64_t* lwork,
+                                        int64_t* lhwork) {
+  if (m < n || n < 1 || nrhs < 1) return LATER_ERR_INVALID_ARG;
+  const SolveNeed s = ls_solve_need(m, n, nrhs, options_from(opt));
+  if (lwork) *lwork = s.work;
+  if (lhwork) *lhwork = s.hwork;
+  return LATER_OK;
+}
+
+later_status_t later_c_ls_solve(later_stream_t stream, int m, int n, int nrhs, const float* A, int lda,
+                                const float* B, int ldb, double* X, int ldx, float* work, int64_t lwork,
+                                void* hwork, int64_t lhwork, const later_options_t* opt, int max_iter, double tol,
+                                later_solve_info_t* info) {
+  SolveInfo si;
+  const later_status_t s = ls_solve(reinterpret_cast<cudaStream_t>(stream), m, n, nrhs, A, lda, B, ldb, X, ldx, work,
+                                    lwork, hwork, lhwork, options_from(opt), max_iter, tol, &si);
+  if (info) {
+    info->iterations = si.iterations;
+    info->factor_precision = si.factor_precision;
+    info->backward_error = si.backward_error;
+  }
+  return s;
+}
+
+}  // extern "C"
+
+namespace later {
+int64_t batched_plan_bytes(int count);
+later_status_t batched_plan(cudaStream_t st, int count, const later_qr_item_t* host_items, void* plan,
+                            int64_t plan_bytes);
+later_status_t batched_run(cudaStream_t st, int count, const void* plan, int* queue, int* status, int variant);
+}  // namespace later
+
+extern "C" {
+
+int64_t later_c_batched_plan_bytes(int count) { return count > 0 ? batched_plan_bytes(count) : 0; }
+
+later_status_t later_c_batched_qr_plan(later_stream_t stream, int count, const later_qr_item_t* items, void* plan,
+                                       int64_t plan_bytes) {
+  return batched_plan(reinterpret_cast<cudaStream_t>(stream), count, items, plan, plan_bytes);
+}
+
+later_status_t later_c_batched_qr_run(later_stream_t stream, int count, const void* plan, int* queue, int* status,
+                                      int variant) {
+  if (variant < -1 || variant > 3) return LATER_ERR_INVALID_ARG;
+  return batched_run(reinterpret_cast<cudaStream_t>(stream), count, plan, queue, status, variant < 0 ? 0 : variant);
 }
 
 later_status_t later_c_gemm16(later_stream_t stream, char transa, char transb, int m, int n, int k, float alpha,

@@ -8,7 +8,7 @@
 // FP32 cublasSgemm block-CGS updates (QR/panel.cu:10-63).
 //
 // Here the whole reduction tree is one launch (tsqr_reduce_kernel): every CTA
-// factors its 256-row block with MGS held in registers (warp = column),
+// factors its 256-row block with block MGS held in registers (4 columns per warp),
 // writes Q in place and its R into the next level's stack, then takes an
 // atomic ticket; the last CTA of each group of eight carries on with the next
 // level, so no CTA ever waits on another CTA. A second launch
@@ -33,7 +33,7 @@ constexpr int PB = 32;       // panel width
 constexpr int BR = 256;      // rows per TSQR block at every level
 constexpr int RPL = BR / 32; // rows per lane
 constexpr int kGroup = BR / PB;  // blocks of one level stacked into a block of the next (8)
-constexpr int APPLY_ROWS = 256;
+constexpr int APPLY_ROWS = 128;
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -41,54 +41,105 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-// MGS of one (<= 256) x 32 block held in registers: warp w owns column w,
-// lane l holds rows l + 32 t. One barrier per step (q_k is double-buffered in
-// shared memory). Squared column norms are downdated by Pythagoras
-// (s -= d^2) after each projection, so the critical path of a step has one
-// warp reduction; when a column has lost more than half of its squared norm
-// the norm is recomputed exactly (no cancellation). Columns beyond the
-// block's row count are exactly dependent: q = 0, zero R row.
-__device__ void mgs_block(float (&a)[RPL], int mm, float* qbuf /*2 x 256*/, float* Rs /*32 x 33*/) {
+// Block MGS of one (<= 256) x 32 block held in registers: 8 warps, warp w
+// owns columns 4w .. 4w+3, lane l holds rows l + 32 t (t < 8) of them. Block
+// step K: warp K orthonormalises its four columns with MGS using warp
+// shuffles only, publishes the four q vectors in shared memory; after one
+// barrier every later warp projects its four columns against the four new q
+// (16 independent warp reductions in flight). Eight barriers per block
+// instead of 32. Columns beyond the block's row count are exactly dependent:
+// q = 0 and a zero R row.
+constexpr int CPW = 4;  // columns per warp
+
+__device__ __forceinline__ float warp_sum4(float v) { return warp_sum(v); }
+
+__device__ void bmgs_block(float (&a)[CPW][RPL], int mm, float* qbuf /*2 x CPW x BR*/, float* Rs /*32 x 33*/) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  float s0 = 0.f;
-#pragma unroll
-  for (int t = 0; t < RPL; ++t) s0 += a[t] * a[t];
-  s0 = warp_sum(s0);
-  float s = s0;
 #pragma unroll 1
-  for (int k = 0; k < PB; ++k) {
-    float* q = qbuf + (k & 1) * BR;
-    if (w == k) {
-      if (!(s > 0.5f * s0)) {
-        s = 0.f;
+  for (int K = 0; K < PB / CPW; ++K) {
+    float* qb = qbuf + (K & 1) * CPW * BR;
+    if (w == K) {
 #pragma unroll
-        for (int t = 0; t < RPL; ++t) s += a[t] * a[t];
-        s = warp_sum(s);
-      }
-      float nrm = sqrtf(fmaxf(s, 0.f));
-      if (k >= mm || !(nrm > 0.f)) nrm = 0.f;
-      const float inv = nrm > 0.f ? 1.f / nrm : 0.f;
+      for (int j = 0; j < CPW; ++j) {
+        const int c = CPW * K + j;
+        float ss = 0.f;
 #pragma unroll
-      for (int t = 0; t < RPL; ++t) {
-        a[t] *= inv;
-        q[l + 32 * t] = a[t];
+        for (int t = 0; t < RPL; ++t) ss += a[j][t] * a[j][t];
+        ss = warp_sum(ss);
+        float nrm = sqrtf(ss);
+        if (c >= mm || !(nrm > 0.f)) nrm = 0.f;
+        const float inv = nrm > 0.f ? 1.f / nrm : 0.f;
+#pragma unroll
+        for (int t = 0; t < RPL; ++t) a[j][t] *= inv;
+        if (l == 0) Rs[c * 33 + c] = nrm;
+        float d[CPW];
+#pragma unroll
+        for (int jj = 0; jj < CPW; ++jj) {
+          d[jj] = 0.f;
+          if (jj > j) {
+#pragma unroll
+            for (int t = 0; t < RPL; ++t) d[jj] += a[j][t] * a[jj][t];
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+          for (int jj = 0; jj < CPW; ++jj)
+            if (jj > j) d[jj] += __shfl_xor_sync(0xffffffffu, d[jj], o);
+#pragma unroll
+        for (int jj = 0; jj < CPW; ++jj)
+          if (jj > j) {
+#pragma unroll
+            for (int t = 0; t < RPL; ++t) a[jj][t] -= d[jj] * a[j][t];
+            if (l == 0) Rs[c * 33 + CPW * K + jj] = d[jj];
+          }
       }
-      if (l == 0) Rs[k * 33 + k] = nrm;
+#pragma unroll
+      for (int j = 0; j < CPW; ++j)
+#pragma unroll
+        for (int t = 0; t < RPL; ++t) qb[j * BR + l + 32 * t] = a[j][t];
     }
     __syncthreads();
-    if (w > k) {
-      float qv[RPL];
-      float d = 0.f;
+    if (w > K) {
+      float d[CPW][CPW];  // d[i][j] = q_i . a_j
+#pragma unroll
+      for (int i = 0; i < CPW; ++i)
+#pragma unroll
+        for (int j = 0; j < CPW; ++j) d[i][j] = 0.f;
 #pragma unroll
       for (int t = 0; t < RPL; ++t) {
-        qv[t] = q[l + 32 * t];
-        d += qv[t] * a[t];
-      }
-      d = warp_sum(d);
 #pragma unroll
-      for (int t = 0; t < RPL; ++t) a[t] -= d * qv[t];
-      s -= d * d;
-      if (l == 0) Rs[k * 33 + w] = d;  // R[k][w]
+        for (int i = 0; i < CPW; ++i) {
+          const float q = qb[i * BR + l + 32 * t];
+#pragma unroll
+          for (int j = 0; j < CPW; ++j) d[i][j] += q * a[j][t];
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < CPW; ++i)
+#pragma unroll
+          for (int j = 0; j < CPW; ++j) d[i][j] += __shfl_xor_sync(0xffffffffu, d[i][j], o);
+#pragma unroll
+      for (int t = 0; t < RPL; ++t) {
+#pragma unroll
+        for (int i = 0; i < CPW; ++i) {
+          const float q = qb[i * BR + l + 32 * t];
+#pragma unroll
+          for (int j = 0; j < CPW; ++j) a[j][t] -= d[i][j] * q;
+        }
+      }
+      if (l < CPW * CPW) {
+        const int i = l / CPW, j = l % CPW;
+        float v = 0.f;
+#pragma unroll
+        for (int ii = 0; ii < CPW; ++ii)
+#pragma unroll
+          for (int jj = 0; jj < CPW; ++jj)
+            if (ii == i && jj == j) v = d[ii][jj];
+        Rs[(CPW * K + i) * 33 + CPW * w + j] = v;  // R[row of q_i][column of a_j]
+      }
     }
   }
   __syncthreads();
@@ -97,8 +148,8 @@ __device__ void mgs_block(float (&a)[RPL], int mm, float* qbuf /*2 x 256*/, floa
 // Whole TSQR reduction tree in one launch. Each CTA factors one level-0 block;
 // the last CTA of each group (atomic ticket) factors the group's stacked R at
 // the next level, and so on up to the root. Q factors stay in place.
-__global__ void __launch_bounds__(1024, 1) tsqr_reduce_kernel(TsqrPlan P) {
-  __shared__ float qbuf[2 * BR];
+__global__ void __launch_bounds__(256) tsqr_reduce_kernel(TsqrPlan P) {
+  __shared__ float qbuf[2 * CPW * BR];
   __shared__ float Rs[PB * 33];
   __shared__ int last;
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -109,22 +160,35 @@ __global__ void __launch_bounds__(1024, 1) tsqr_reduce_kernel(TsqrPlan P) {
     const int64_t ld = P.ld[L];
     const int r0 = b * BR;
     const int mm = min(BR, P.rows[L] - r0);
-    float a[RPL];
+    // Columns at or beyond P.ncols do not exist at level 0 (read as zero, never
+    // written); the stacked levels always carry 32 columns.
+    const int ncols = (L == 0) ? P.ncols : PB;
+    float a[CPW][RPL];
 #pragma unroll
-    for (int t = 0; t < RPL; ++t) {
-      const int r = l + 32 * t;
-      a[t] = (r < mm) ? __ldcg(&X[r0 + r + static_cast<int64_t>(w) * ld]) : 0.f;
-    }
-    mgs_block(a, mm, qbuf, Rs);
+    for (int j = 0; j < CPW; ++j)
 #pragma unroll
-    for (int t = 0; t < RPL; ++t) {
-      const int r = l + 32 * t;
-      if (r < mm) X[r0 + r + static_cast<int64_t>(w) * ld] = a[t];
-    }
+      for (int t = 0; t < RPL; ++t) {
+        const int r = l + 32 * t;
+        const int col = CPW * w + j;
+        a[j][t] = (r < mm && col < ncols) ? __ldcg(&X[r0 + r + static_cast<int64_t>(col) * ld]) : 0.f;
+      }
+    bmgs_block(a, mm, qbuf, Rs);
+#pragma unroll
+    for (int j = 0; j < CPW; ++j)
+#pragma unroll
+      for (int t = 0; t < RPL; ++t) {
+        const int r = l + 32 * t;
+        const int col = CPW * w + j;
+        if (r < mm && col < ncols) X[r0 + r + static_cast<int64_t>(col) * ld] = a[j][t];
+      }
     const bool root = (P.nblk[L] == 1);
     float* Ro = root ? P.R : P.lev[L + 1] + 32 * b;
     const int64_t ldo = root ? P.ldr : P.ld[L + 1];
-    Ro[l + static_cast<int64_t>(w) * ldo] = (l <= w) ? Rs[l * 33 + w] : 0.f;
+    const int rcols = root ? P.ncols : PB;
+    for (int e = threadIdx.x; e < PB * PB; e += blockDim.x) {
+      const int i = e % PB, j = e / PB;
+      if (i < rcols && j < rcols) Ro[i + static_cast<int64_t>(j) * ldo] = (i <= j) ? Rs[i * 33 + j] : 0.f;
+    }
     if (root) break;
     __threadfence();
     __syncthreads();
@@ -146,35 +210,44 @@ __global__ void __launch_bounds__(1024, 1) tsqr_reduce_kernel(TsqrPlan P) {
 
 // Each CTA finishes 256 rows of Q: T = product of its 32x32 path slices
 // through the tree, Q = Q0 * T, written in FP32 and as the 16-bit copy.
-__global__ void __launch_bounds__(256) tsqr_apply_kernel(TsqrPlan P, void* qh, void* ql, int64_t ldh,
-                                                         int out_mode) {
+__global__ void __launch_bounds__(APPLY_ROWS) tsqr_apply_kernel(TsqrPlan P, void* qh, void* ql, int64_t ldh,
+                                                                int out_mode) {
   __shared__ float T[PB * 33];
   __shared__ float U[PB * 33];
   const int row0 = blockIdx.x * APPLY_ROWS;
   const int b = row0 / P.br[0];  // level-0 block
   const int tid = threadIdx.x;
   const int top = P.nlev - 1;
+  // This thread's row of Q0, loaded before the path composition so the loads overlap it.
+  const int row = row0 + tid;
+  const bool has_row = row < P.rows[0];
+  float* X = P.lev[0];
+  const int64_t ld = P.ld[0];
+  float q[PB];
+#pragma unroll
+  for (int k = 0; k < PB; ++k) q[k] = (has_row && k < P.ncols) ? __ldcg(&X[row + static_cast<int64_t>(k) * ld]) : 0.f;
   // Index at level L of the level-0 block b: b / div[L].
   if (top == 0) {
-    for (int e = tid; e < PB * PB; e += 256) T[(e % PB) * 33 + e / PB] = (e % PB == e / PB) ? 1.f : 0.f;
+    for (int e = tid; e < PB * PB; e += APPLY_ROWS) T[(e % PB) * 33 + e / PB] = (e % PB == e / PB) ? 1.f : 0.f;
   } else {
     const int bt = b / P.div[top - 1];  // block index at level top-1
-    for (int e = tid; e < PB * PB; e += 256) {
+    for (int e = tid; e < PB * PB; e += APPLY_ROWS) {
       const int i = e % PB, j = e / PB;
       T[i * 33 + j] = __ldcg(&P.lev[top][32 * bt + i + static_cast<int64_t>(j) * P.ld[top]]);
     }
     for (int L = top - 1; L >= 1; --L) {
       __syncthreads();
       const int bl = b / P.div[L - 1];
-      for (int e = tid; e < PB * PB; e += 256) {  // stage the 32x32 slice
+      for (int e = tid; e < PB * PB; e += APPLY_ROWS) {  // stage the 32x32 slice
         const int i = e % PB, j = e / PB;
         U[i * 33 + j] = __ldcg(&P.lev[L][32 * bl + i + static_cast<int64_t>(j) * P.ld[L]]);
       }
       __syncthreads();
-      float out[4];
+      constexpr int PER = PB * PB / APPLY_ROWS;
+      float out[PER];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int e = tid + 256 * u;
+      for (int u = 0; u < PER; ++u) {
+        const int e = tid + APPLY_ROWS * u;
         const int i = e % PB, j = e / PB;
         float acc = 0.f;
 #pragma unroll
@@ -183,22 +256,17 @@ __global__ void __launch_bounds__(256) tsqr_apply_kernel(TsqrPlan P, void* qh, v
       }
       __syncthreads();
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int e = tid + 256 * u;
+      for (int u = 0; u < PER; ++u) {
+        const int e = tid + APPLY_ROWS * u;
         T[(e % PB) * 33 + e / PB] = out[u];
       }
     }
   }
   __syncthreads();
-  const int row = row0 + tid;
-  if (row >= P.rows[0]) return;
-  float* X = P.lev[0];
-  const int64_t ld = P.ld[0];
-  float q[PB];
-#pragma unroll
-  for (int k = 0; k < PB; ++k) q[k] = __ldcg(&X[row + static_cast<int64_t>(k) * ld]);
+  if (!has_row) return;
 #pragma unroll 4
   for (int j = 0; j < PB; ++j) {
+    if (j >= P.ncols) break;
     float s = 0.f;
 #pragma unroll
     for (int k = 0; k < PB; ++k) s += q[k] * T[k * 33 + j];
@@ -275,7 +343,7 @@ __global__ void __launch_bounds__(256) tn_partial_kernel(int m, int rpc, int k1,
 // slice j sums chunks j, j+8, ... in order, slices combined in a fixed tree.
 __global__ void __launch_bounds__(256) tn_reduce_kernel(int nch, int ntiles, int k1, int k2,
                                                         const float* __restrict__ part, float* R, int64_t ldr,
-                                                        int accumulate) {
+                                                        int accumulate, float alpha) {
   __shared__ float sl[8][33];
   const int t = blockIdx.x / 128;                     // output tile
   const int e = (blockIdx.x % 128) * 32 + threadIdx.x % 32;  // element of the 64x64 tile
@@ -292,7 +360,7 @@ __global__ void __launch_bounds__(256) tn_reduce_kernel(int nch, int ntiles, int
   const int i = (t % ti_n) * 64 + e % 64, jj = (t / ti_n) * 64 + e / 64;
   if (i >= k1 || jj >= k2) return;
   float* o = &R[i + static_cast<int64_t>(jj) * ldr];
-  *o = accumulate ? *o + s : s;
+  *o = accumulate ? *o + alpha * s : alpha * s;
 }
 
 // Y[rows, cols] -= X[rows, :] * S[:, cols] with S (k1 x k2). One CTA per 64
@@ -406,8 +474,10 @@ void tsqr_plan_sizes(int m, TsqrPlan* P, int64_t* stack_floats, int* ncounters) 
 }
 
 later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R, int64_t ldr, void* qh, void* ql,
-                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed, long long budget) {
+                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed, long long budget, int ncols) {
+  if (ncols < 1 || ncols > PB) return LATER_ERR_INVALID_ARG;
   TsqrPlan P{};
+  P.ncols = ncols;
   int64_t stack = 0;
   int ncnt = 0;
   tsqr_plan_sizes(m, &P, &stack, &ncnt);
@@ -430,11 +500,11 @@ later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R
     return LATER_OK;
   }
   TraceScope trace(s, TRACE_PANEL);
-  tsqr_reduce_kernel<<<P.nblk[0], 1024, 0, s>>>(P);
+  tsqr_reduce_kernel<<<P.nblk[0], 256, 0, s>>>(P);
   note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
   const int mode = out_prec == LATER_PREC_BF16 ? 1 : (out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
-  tsqr_apply_kernel<<<(m + APPLY_ROWS - 1) / APPLY_ROWS, 256, 0, s>>>(P, qh, ql, ldh, mode);
+  tsqr_apply_kernel<<<(m + APPLY_ROWS - 1) / APPLY_ROWS, APPLY_ROWS, 0, s>>>(P, qh, ql, ldh, mode);
   note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
   ws.reset(mark);
@@ -442,7 +512,7 @@ later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R
 }
 
 later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* Y,
-                       int64_t ldy, float* R, int64_t ldr, int accumulate, Arena& ws) {
+                       int64_t ldy, float* R, int64_t ldr, int accumulate, Arena& ws, float alpha) {
   if (m <= 0 || k1 <= 0 || k2 <= 0) return LATER_OK;
   // Partial 64x64 tiles per (row chunk, output tile); as many row chunks (up
   // to one per 128 rows, at most 256) as the workspace holds.
@@ -465,7 +535,7 @@ later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, in
   tn_partial_kernel<<<dim3(nch, ntiles), 256, 0, s>>>(m, rpc, k1, k2, X, ldx, Y, ldy, part);
   note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
-  tn_reduce_kernel<<<ntiles * 128, 256, 0, s>>>(nch, ntiles, k1, k2, part, R, ldr, accumulate);
+  tn_reduce_kernel<<<ntiles * 128, 256, 0, s>>>(nch, ntiles, k1, k2, part, R, ldr, accumulate, alpha);
   note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
   ws.reset(mark);

@@ -25,18 +25,22 @@ struct TsqrPlan {
   int64_t ldr;
   int* status;
   long long budget;
+  int ncols;  // columns of the level-0 panel (<= 32)
 };
 
 void tsqr_plan_sizes(int m, TsqrPlan* P, int64_t* stack_floats, int* ncounters);
 
-// QR of the m x 32 panel A: Q overwrites A (FP32) and is also written to the
-// 16-bit copy (qh / ql, may be null); R (32x32, upper) goes to R.
+// QR of the m x ncols panel A (ncols <= 32): Q overwrites A (FP32) and is also
+// written to the 16-bit copy (qh / ql, may be null); R (ncols x ncols, upper)
+// goes to R.
 later_status_t tsqr_panel(cudaStream_t s, int m, float* A, int64_t lda, float* R, int64_t ldr, void* qh, void* ql,
-                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed, long long budget);
+                          int64_t ldh, int out_prec, Arena& ws, int* counters_zeroed, long long budget,
+                          int ncols = 32);
 
-// R (+)= X^T Y for X (m x k1), Y (m x k2), FP32 (SIMT, deterministic split over rows).
+// R = alpha X^T Y (+ R when accumulate) for X (m x k1), Y (m x k2), FP32
+// (SIMT, deterministic split over rows).
 later_status_t simt_tn(cudaStream_t s, int m, int k1, int k2, const float* X, int64_t ldx, const float* Y,
-                       int64_t ldy, float* R, int64_t ldr, int accumulate, Arena& ws);
+                       int64_t ldy, float* R, int64_t ldr, int accumulate, Arena& ws, float alpha = 1.f);
 
 // Y -= X S for X (m x k1), S (k1 x k2), FP32 (SIMT); optional 16-bit copy of
 // the updated Y (yh / yl with leading dimension ldh, format out_prec).

@@ -71,7 +71,7 @@ Scratch gemm_scratch(Ctx& c) {
 later_status_t leaf_qr(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
   if (w <= 32) {
     return tsqr_panel(c.st, c.m, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
-                      c.o.prec, *c.ws, c.counters, c.o.budget);
+                      c.o.prec, *c.ws, c.counters, c.o.budget, w);
   }
   const int w1 = split_half(w), w2 = w - w1;
   LATER_CHECK(leaf_qr(c, w1, A, lda, R, ldr, col));
@@ -201,7 +201,7 @@ QrNeed rgsqrf_need(int m, int n, const Options& o) {
 
 later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, float* R, int64_t ldr, float* work,
                       int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
-  if (m < 1 || n < 1 || m < n || n % 32 != 0 || lda < m || ldr < n || !A || !R) return LATER_ERR_INVALID_ARG;
+  if (m < 1 || n < 1 || m < n || lda < m || ldr < n || !A || !R) return LATER_ERR_INVALID_ARG;
   if (o.leaf != 32 && o.leaf != 64 && o.leaf != 128) return LATER_ERR_INVALID_ARG;
   if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;
   const QrNeed need = rgsqrf_need(m, n, o);

@@ -79,6 +79,13 @@ def test_rgsqrf_rejects_bad_args(cuda):
     A = lg.empty_colmajor(100, 200)
     with pytest.raises(lg.LaterError):
         lg.later_rgsqrf(A)  # m < n
-    A = lg.empty_colmajor(256, 100)
-    with pytest.raises(lg.LaterError):
-        lg.later_rgsqrf(A)  # n not a multiple of 32
+
+
+@pytest.mark.parametrize("m,n", [(1000, 100), (700, 17), (4096, 333)])
+def test_rgsqrf_any_width(cuda, m, n):
+    A = gen.normal(m, n, seed=n)
+    Q, R = run_gpu(A)
+    Qo, Ro = lo.rgsqrf(A)
+    assert metrics.qr_backward_error(A, Q, R) <= max(3 * metrics.qr_backward_error(A, Qo, Ro), 1e-6)
+    assert metrics.orthogonality(Q) <= max(3 * metrics.orthogonality(Qo), 1e-5)
+    assert np.all(np.tril(R, -1) == 0) and np.all(np.diag(R) > 0)
