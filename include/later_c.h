@@ -195,6 +195,52 @@ later_status_t later_c_ls_solve(later_stream_t stream, int m, int n, int nrhs, c
                                 void* hwork, int64_t lhwork, const later_options_t* opt, int max_iter, double tol,
                                 later_solve_info_t* info);
 
+/* ------------------------------------------------ least-squares serving */
+/* No counterpart in the reference. A server owns one device, `slots` worker
+ * threads with one CUDA stream each, and an HBM budget (one allocation made at
+ * creation, carved per request by a first-fit pool). Requests (host A, B; the
+ * FP64 solution X is written back to host memory) queue FIFO; a free worker
+ * admits the head request as soon as the pool holds everything it needs, so
+ * requests arriving while others run are admitted as slots and memory free
+ * up and their kernels overlap on the device. Each request runs
+ * later_c_ls_solve's algorithm (QR factors stay in HBM for the whole solve). */
+
+typedef struct later_server later_server_t;
+
+typedef struct {
+  int m, n, nrhs, reserved; /* m >= n >= 32, nrhs <= 16 */
+  const float* A;           /* host, column-major m x n */
+  const float* B;           /* host, m x nrhs */
+  double* X;                /* host, n x nrhs, receives the solution */
+  int lda, ldb, ldx, reserved2;
+} later_ls_request_t;
+
+typedef struct {
+  int status;               /* later_status_t of the solve */
+  int iterations;
+  int slot;                 /* worker that served it */
+  int reserved;
+  double backward_error;
+  double submit_ms;         /* submit time since server creation */
+  double queue_ms;          /* submit -> admitted */
+  double service_ms;        /* admitted -> done */
+  double latency_ms;        /* submit -> done */
+} later_ls_result_t;
+
+/* Returns NULL on failure (bad arguments or the budget allocation failed). */
+later_server_t* later_c_ls_server_create(int device, int slots, int64_t hbm_budget_bytes,
+                                         const later_options_t* opt, int max_iter, double tol);
+/* Queues a request; returns a ticket >= 0, or -later_status_t (a request
+ * larger than the whole budget is refused with -LATER_ERR_WORKSPACE). The
+ * host buffers must stay valid until later_c_ls_server_wait returns. */
+int64_t later_c_ls_server_submit(later_server_t* s, const later_ls_request_t* req);
+/* Blocks until the request is done and fills `out`. */
+later_status_t later_c_ls_server_wait(later_server_t* s, int64_t ticket, later_ls_result_t* out);
+/* Bytes of the HBM budget currently held by admitted requests. */
+int64_t later_c_ls_server_hbm_in_use(later_server_t* s);
+/* Drains the queue, joins the workers and frees the budget. */
+void later_c_ls_server_destroy(later_server_t* s);
+
 /* ---------------------------------------------------------- batched QR */
 /* No counterpart in the reference. Many independent FP32 matrices of uneven
  * sizes (m >= n, n <= 256) factored A_i = Q_i R_i in one persistent-kernel

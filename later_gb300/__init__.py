@@ -21,7 +21,7 @@ __all__ = [
     "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
     "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "later_rsyrk", "later_rtrsm",
     "later_rtrmm", "later_rpotrf", "blas3_bufsize",
-    "spd_solve", "ls_solve", "BatchedQR", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
+    "spd_solve", "ls_solve", "BatchedQR", "LsServer", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
     "trace_end",
 ]
 
@@ -45,6 +45,42 @@ class Options(ctypes.Structure):
     def make(cls, precision="fp16", cgs2=False, leaf=128, timeout_cycles=0) -> "Options":
         p = PREC[precision] if isinstance(precision, str) else int(precision)
         return cls(p, int(bool(cgs2)), int(leaf), 0, int(timeout_cycles))
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("factor_precision", ctypes.c_int), ("backward_error", ctypes.c_double)]
+
+
+class QrItem(ctypes.Structure):
+    _fields_ = [("A", ctypes.c_void_p), ("R", ctypes.c_void_p), ("lda", ctypes.c_int64), ("ldr", ctypes.c_int64),
+                ("m", ctypes.c_int), ("n", ctypes.c_int)]
+
+
+class LsRequest(ctypes.Structure):
+    _fields_ = [("m", ctypes.c_int), ("n", ctypes.c_int), ("nrhs", ctypes.c_int), ("reserved", ctypes.c_int),
+                ("A", ctypes.c_void_p), ("B", ctypes.c_void_p), ("X", ctypes.c_void_p),
+                ("lda", ctypes.c_int), ("ldb", ctypes.c_int), ("ldx", ctypes.c_int), ("reserved2", ctypes.c_int)]
+
+
+class LsResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("slot", ctypes.c_int),
+                ("reserved", ctypes.c_int), ("backward_error", ctypes.c_double), ("submit_ms", ctypes.c_double),
+                ("queue_ms", ctypes.c_double), ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
+
+
+class Trace(ctypes.Structure):
+    _fields_ = [("gemm_flops", ctypes.c_double), ("gemm_ms", ctypes.c_double), ("gemm_launches", ctypes.c_int64),
+                ("top_gemm_flops", ctypes.c_double), ("top_gemm_ms", ctypes.c_double),
+                ("panel_ms", ctypes.c_double), ("panel_launches", ctypes.c_int64),
+                ("leaf_gemm_flops", ctypes.c_double), ("leaf_gemm_ms", ctypes.c_double),
+                ("leaf_gemm_launches", ctypes.c_int64), ("other_ms", ctypes.c_double),
+                ("other_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _lib = None
@@ -74,31 +110,15 @@ _SIGS = {
     "later_c_batched_plan_bytes": (_i64, [_i]),
     "later_c_batched_qr_plan": (_i, [_vp, _i, _vp, _vp, _i64]),
     "later_c_batched_qr_run": (_i, [_vp, _i, _vp, _vp, _vp, _i]),
+    "later_c_ls_server_create": (_vp, [_i, _i, _i64, ctypes.POINTER(Options), _i, ctypes.c_double]),
+    "later_c_ls_server_submit": (_i64, [_vp, ctypes.POINTER(LsRequest)]),
+    "later_c_ls_server_wait": (_i, [_vp, _i64, ctypes.POINTER(LsResult)]),
+    "later_c_ls_server_hbm_in_use": (_i64, [_vp]),
+    "later_c_ls_server_destroy": (None, [_vp]),
     "later_c_launch_count": (ctypes.c_uint64, []),
     "later_c_trace_begin": (None, []),
     "later_c_trace_end": (_i, [_vp]),
 }
-
-
-class SolveInfo(ctypes.Structure):
-    _fields_ = [("iterations", ctypes.c_int), ("factor_precision", ctypes.c_int), ("backward_error", ctypes.c_double)]
-
-
-class QrItem(ctypes.Structure):
-    _fields_ = [("A", ctypes.c_void_p), ("R", ctypes.c_void_p), ("lda", ctypes.c_int64), ("ldr", ctypes.c_int64),
-                ("m", ctypes.c_int), ("n", ctypes.c_int)]
-
-
-class Trace(ctypes.Structure):
-    _fields_ = [("gemm_flops", ctypes.c_double), ("gemm_ms", ctypes.c_double), ("gemm_launches", ctypes.c_int64),
-                ("top_gemm_flops", ctypes.c_double), ("top_gemm_ms", ctypes.c_double),
-                ("panel_ms", ctypes.c_double), ("panel_launches", ctypes.c_int64),
-                ("leaf_gemm_flops", ctypes.c_double), ("leaf_gemm_ms", ctypes.c_double),
-                ("leaf_gemm_launches", ctypes.c_int64), ("other_ms", ctypes.c_double),
-                ("other_launches", ctypes.c_int64)]
-
-    def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 def lib_path() -> Path:
@@ -388,6 +408,56 @@ class BatchedQR:
                                             self.queue.data_ptr(), self.status.data_ptr(), int(variant)),
                "batched_qr_run")
         return self.rs
+
+
+class LsServer:
+    """Continuous-batching least-squares server (native C++ workers; see later_c.h).
+
+    submit(A, B) takes column-major float32 numpy arrays (host) and returns a ticket;
+    wait(ticket) returns (X float64 (n x nrhs), result dict with latency figures).
+    """
+
+    def __init__(self, slots=4, hbm_budget_gb=16.0, precision="split3", max_iter=30, tol=1e-6, device=0):
+        o = Options.make(precision)
+        self._h = lib().later_c_ls_server_create(device, slots, int(hbm_budget_gb * (1 << 30)), ctypes.byref(o),
+                                                 max_iter, tol)
+        if not self._h:
+            raise LaterError(3, "later_c_ls_server_create")
+        self._keep = {}
+
+    def submit(self, A, B):
+        import numpy as np
+        A = np.asfortranarray(A, dtype=np.float32)
+        B = np.asfortranarray(B.reshape(B.shape[0], -1), dtype=np.float32)
+        m, n = A.shape
+        k = B.shape[1]
+        X = np.zeros((n, k), dtype=np.float64, order="F")
+        req = LsRequest(m, n, k, 0, A.ctypes.data, B.ctypes.data, X.ctypes.data, m, m, n, 0)
+        t = lib().later_c_ls_server_submit(self._h, ctypes.byref(req))
+        if t < 0:
+            raise LaterError(int(-t), "later_c_ls_server_submit")
+        self._keep[t] = (A, B, X)
+        return t
+
+    def wait(self, ticket):
+        res = LsResult()
+        _check(lib().later_c_ls_server_wait(self._h, ticket, ctypes.byref(res)), "later_c_ls_server_wait")
+        A, B, X = self._keep.pop(ticket)
+        return X, res.as_dict()
+
+    def hbm_in_use(self):
+        return int(lib().later_c_ls_server_hbm_in_use(self._h))
+
+    def close(self):
+        if self._h:
+            lib().later_c_ls_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def gemm16(transa, transb, A, B, alpha=1.0, beta=0.0, C=None, D=None, precision="fp16", work=None, stream=None):

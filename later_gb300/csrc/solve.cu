@@ -355,7 +355,7 @@ later_status_t spd_solve(cudaStream_t st, int n, int k, const float* A, int64_t 
 later_status_t ls_solve(cudaStream_t st, int m, int n, int k, const float* A, int64_t lda, const float* B,
                         int64_t ldb, double* X, int64_t ldx, float* work, int64_t lwork, void* hwork, int64_t lhwork,
                         const Options& o, int max_iter, double tol, SolveInfo* info) {
-  if (m < n || n < 32 || n % 32 || k < 1 || k > RK || !A || !B || !X || lda < m || ldb < m || ldx < n)
+  if (m < n || n < 1 || k < 1 || k > RK || !A || !B || !X || lda < m || ldb < m || ldx < n)
     return LATER_ERR_INVALID_ARG;
   const SolveNeed need = ls_solve_need(m, n, k, o);
   if (!work || !hwork || lwork < need.work || lhwork < need.hwork) return LATER_ERR_WORKSPACE;
