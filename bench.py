@@ -57,6 +57,14 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--cpu-m", type=int, default=16384, help="CPU sample rows")
     p.add_argument("--cpu-n", type=int, default=1024, help="CPU sample columns")
+    p.add_argument("--config", default="qr", choices=["qr", "spd", "batched", "serve"],
+                   help="qr: rgsqrf (default, the headline); spd: rpotrf + FP64-refined SPD solve; "
+                        "batched: 4096 uneven tall-skinny QRs in one persistent launch; serve: LS serving loop")
+    p.add_argument("--kappa", type=float, default=1e2, help="spd: condition number")
+    p.add_argument("--count", type=int, default=4096, help="batched: number of matrices")
+    p.add_argument("--rates", type=float, nargs="*", default=None, help="serve: arrival rates (req/s)")
+    p.add_argument("--requests", type=int, default=64, help="serve: requests per rate")
+    p.add_argument("--slots", type=int, default=4, help="serve: server slots")
     p.add_argument("--gemm", type=int, nargs=3, metavar=("M", "N", "K"), default=None,
                    help="time only the tensor-core GEMM R12 = Q1^T A2 of this shape (TN, FP16) — the "
                         "top-level trailing-update product of rgsqrf; used for kernel profiling")
@@ -350,10 +358,229 @@ def run_gemm_only(a):
                       "unit": "TFLOP/s", "ms_per_step": ms, "shape": [M, N, K], "op": "TN fp16->fp32"}), flush=True)
 
 
+def _haar_gpu(n, k, g):
+    import torch
+    q, r = torch.linalg.qr(torch.randn(n, k, generator=g, device="cuda", dtype=torch.float64))
+    return q * torch.sign(torch.diagonal(r))[None, :]
+
+
+def run_spd(a):
+    """Config 3: n x n SPD A = Q diag(lambda) Q^T (Q Haar, lambda log-uniform in [1/kappa, 1]),
+    rpotrf + FP64 iterative refinement on 16 FP32 right-hand sides to backward error 1e-12."""
+    import numpy as np
+    import torch
+    import later_gb300 as lg
+    n, k = a.n, 16
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    # Q from an FP32 QR (an FP64 QR of n=16384 is slow on GB300's FP64 units); A = Q diag(lam) Q^T is formed
+    # in FP64, so A is a congruence of diag(lam) by a near-orthogonal Q (spectrum within ~1e-5 relative) and
+    # only its final rounding to FP32 perturbs it. An FP32 product would add accumulation error far above
+    # lam_min = 1/kappa at kappa = 1e6.
+    q, r = torch.linalg.qr(torch.randn(n, n, generator=g, device="cuda"))
+    q *= torch.sign(torch.diagonal(r))[None, :]
+    del r
+    q = q.double()
+    lam = torch.exp(torch.empty(n, device="cuda", dtype=torch.float64).uniform_(-float(np.log(a.kappa)), 0.0,
+                                                                                 generator=g))
+    A = (q * lam[None, :]) @ q.t()
+    del q
+    A = lg.colmajor(((A + A.t()) / 2).float())
+    B = lg.colmajor(torch.randn(n, k, generator=g, device="cuda"))
+    F = lg.empty_colmajor(n, n)
+    lw, lh = lg.blas3_bufsize("p", n, n, precision=a.precision)
+    work = torch.empty(lw, dtype=torch.float32, device="cuda")
+    hwork = torch.empty(lh, dtype=torch.float16, device="cuda")
+    ts, infos = [], []
+    for it in range(a.warmup + a.steps):
+        F.copy_(A)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lg.later_rpotrf("l", n, F, precision=a.precision, work=work, hwork=hwork)
+        e1.record()
+        torch.cuda.synchronize()
+        st = lg.device_status()
+        if it >= a.warmup:
+            ts.append(e0.elapsed_time(e1))
+    fact_ms = statistics.median(ts)
+    t0 = time.perf_counter()
+    X, info = lg.spd_solve(A, B, precision=a.precision, max_iter=50, tol=1e-12)
+    solve_s = time.perf_counter() - t0
+    flops = n ** 3 / 3.0
+    cpu = None
+    if not a.no_cpu:
+        import scipy.linalg.lapack as la
+        ns = n
+        As = np.asfortranarray(A.cpu().numpy())
+        la.spotrf(As[:512, :512].copy(order="F"))
+        t = time.perf_counter()
+        la.spotrf(As, lower=1, overwrite_a=1)
+        dt = time.perf_counter() - t
+        cpu = {"value": ns ** 3 / 3.0 / dt / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"host LAPACK spotrf (scipy's OpenBLAS, all host cores) on the same {ns}x{ns} matrix, {dt:.2f} s"}
+    print(json.dumps({"metric": "Cholesky TFLOP/s (n^3/3) + refined SPD solve", "value": flops / fact_ms / 1e9,
+                      "unit": "TFLOP/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+                      "ms_per_step": fact_ms, "higher_is_better": True, "dtype": a.precision, "data": "synthetic",
+                      "config": {"workload": f"rpotrf n={n} SPD kappa={a.kappa:g} + FP64 refinement, 16 RHS",
+                                 "n": n, "kappa": a.kappa, "precision": a.precision},
+                      "factor_status": st, "solve": {"seconds_incl_factor": solve_s, **info},
+                      "cpu_baseline": cpu}), flush=True)
+
+
+def run_batched(a):
+    """Config 4: `count` N(0,1) matrices, m log-uniform [256, 8192], n log-uniform [16, 256], m >= 4n;
+    one persistent launch under a captured CUDA graph, tile variant from the autotuner; compared with
+    looping plain rgsqrf per matrix (timed on a sample of the same distribution)."""
+    import numpy as np
+    import torch
+    import later_gb300 as lg
+    from later_gb300 import autotune
+    rng = np.random.default_rng(a.seed)
+    shapes = []
+    while len(shapes) < a.count:
+        m = int(np.exp(rng.uniform(np.log(256), np.log(8192))))
+        n = int(np.exp(rng.uniform(np.log(16), np.log(256))))
+        if m >= 4 * n:
+            shapes.append((m, n))
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    orig = [torch.randn(n, m, generator=g, device="cuda").t() for m, n in shapes]
+    mats = [o.clone() for o in orig]
+    flops = sum(2.0 * n * n * (m - n / 3.0) for m, n in shapes)
+    best, tune_ms = autotune.tune(shapes, use_cache=True)
+    b = lg.BatchedQR(mats)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        b.run(best, stream=s)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=s):
+            b.run(best, stream=s)
+    ts = []
+    for it in range(a.warmup + a.steps):
+        for x, o in zip(mats, orig):
+            x.copy_(o)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        graph.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        if it >= a.warmup:
+            ts.append(e0.elapsed_time(e1))
+    ms = statistics.median(ts)
+    bad = int((b.status != 0).sum())
+    # comparator: plain rgsqrf per matrix on a sample of 256, scaled by flops
+    idx = list(range(0, a.count, max(1, a.count // 256)))
+    sub = [orig[i].clone() for i in idx]
+    for x in sub[:4]:
+        lg.later_rgsqrf(x.clone())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for x in sub:
+        lg.later_rgsqrf(x)
+    torch.cuda.synchronize()
+    loop_s = time.perf_counter() - t0
+    sub_flops = sum(2.0 * shapes[i][1] ** 2 * (shapes[i][0] - shapes[i][1] / 3.0) for i in idx)
+    print(json.dumps({"metric": "batched QR TFLOP/s (sum 2n^2(m-n/3)) and matrices/s", "value": flops / ms / 1e9,
+                      "unit": "TFLOP/s", "matrices_per_s": a.count / ms * 1e3, "ms_per_step": ms,
+                      "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True,
+                      "dtype": "fp32", "data": "synthetic", "graph": True, "variant": best, "autotune_ms": tune_ms,
+                      "matrices_failed": bad,
+                      "config": {"workload": f"{a.count} N(0,1) matrices, m in [256,8192], n in [16,256], m>=4n"},
+                      "comparator_rgsqrf_loop": {"value": sub_flops / loop_s / 1e12, "unit": "TFLOP/s",
+                                                 "matrices_per_s": len(sub) / loop_s,
+                                                 "sample": f"{len(sub)} matrices of the same distribution"}}),
+          flush=True)
+
+
+def run_serve(a):
+    """Config 5: Poisson arrivals of LS requests, m log-uniform [512, 32768], n log-uniform [32, 2048],
+    m >= 2n, kappa log-uniform [1e1, 1e4] (SVD construction), b = A x* + 1e-3 noise; refinement to
+    backward error 1e-6; solves/s and p50/p99 latency at each swept rate, against an FP32 QR least-squares
+    (torch.linalg.lstsq on the GPU: cuSOLVER, TF32 off) on the same request stream."""
+    import numpy as np
+    import torch
+    import later_gb300 as lg
+    torch.backends.cuda.matmul.allow_tf32 = False
+    rng = np.random.default_rng(a.seed)
+    g = torch.Generator(device="cuda").manual_seed(a.seed)
+    pool = []
+    npool = min(a.requests, 32)
+    while len(pool) < npool:
+        m = int(np.exp(rng.uniform(np.log(512), np.log(32768))))
+        n = int(np.exp(rng.uniform(np.log(32), np.log(2048))))
+        if m < 2 * n:
+            continue
+        kappa = float(np.exp(rng.uniform(np.log(10), np.log(1e4))))
+        u = _haar_gpu(m, n, g)
+        v = _haar_gpu(n, n, g)
+        sig = torch.logspace(0, -np.log10(kappa), n, device="cuda", dtype=torch.float64)
+        A = ((u * sig[None, :]) @ v.t()).float()
+        xs = torch.randn(n, 1, generator=g, device="cuda", dtype=torch.float64)
+        B = (A.double() @ xs + 1e-3 * torch.randn(m, 1, generator=g, device="cuda", dtype=torch.float64)).float()
+        pool.append((np.asfortranarray(A.cpu().numpy()), np.asfortranarray(B.cpu().numpy())))
+    # capacity estimate: one request at a time
+    srv = lg.LsServer(slots=a.slots, hbm_budget_gb=64, precision="split3", tol=1e-6)
+    for A, B in pool[:2]:
+        srv.wait(srv.submit(A, B))
+    t0 = time.perf_counter()
+    for A, B in pool[:8]:
+        srv.wait(srv.submit(A, B))
+    serial = (time.perf_counter() - t0) / 8
+    rates = a.rates or [0.5 / serial, 1.0 / serial, 2.0 / serial, 4.0 / serial]
+    results = []
+    for lam in rates:
+        arr = np.cumsum(rng.exponential(1.0 / lam, a.requests))
+        t_start = time.perf_counter()
+        tickets = []
+        for i, t_arr in enumerate(arr):
+            now = time.perf_counter() - t_start
+            if t_arr > now:
+                time.sleep(t_arr - now)
+            A, B = pool[i % len(pool)]
+            tickets.append(srv.submit(A, B))
+        outs = [srv.wait(t) for t in tickets]
+        wall = time.perf_counter() - t_start
+        lat = np.array([r["latency_ms"] for _, r in outs])
+        bwd = max(r["backward_error"] for _, r in outs)
+        results.append({"rate": lam, "solves_per_s": len(outs) / wall, "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99)), "max_backward_error": bwd,
+                        "failed": sum(1 for _, r in outs if r["status"] != 0)})
+    srv.close()
+    # FP32 QR baseline on the same GPU, same stream at the highest rate, one request at a time
+    base = []
+    for A, B in pool[:2]:
+        torch.linalg.lstsq(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat = []
+    for i in range(a.requests):
+        A, B = pool[i % len(pool)]
+        t1 = time.perf_counter()
+        x = torch.linalg.lstsq(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()).solution
+        x.cpu()
+        lat.append((time.perf_counter() - t1) * 1e3)
+    wall = time.perf_counter() - t0
+    base = {"solves_per_s": a.requests / wall, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)),
+            "impl": "torch.linalg.lstsq FP32 on the GPU (cuSOLVER QR), serial"}
+    best = max(results, key=lambda r: r["solves_per_s"])
+    print(json.dumps({"metric": "LS solves/s at backward error <= 1e-6, p50/p99 latency", "value": best["solves_per_s"],
+                      "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "split3",
+                      "data": "synthetic", "slots": a.slots, "sweep": results, "fp32_qr_baseline": base,
+                      "config": {"workload": f"{a.requests} LS requests per rate from a pool of {len(pool)}, "
+                                             "m in [512,32768], n in [32,2048], m>=2n, kappa in [1e1,1e4]"}}),
+          flush=True)
+
+
 def main():
     a = parse()
     if a.gemm:
         run_gemm_only(a)
+        return
+    if a.config != "qr" and a.impl == "ours":
+        {"spd": run_spd, "batched": run_batched, "serve": run_serve}[a.config](a)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -238,6 +238,8 @@ int64_t later_c_ls_server_submit(later_server_t* s, const later_ls_request_t* re
 later_status_t later_c_ls_server_wait(later_server_t* s, int64_t ticket, later_ls_result_t* out);
 /* Bytes of the HBM budget currently held by admitted requests. */
 int64_t later_c_ls_server_hbm_in_use(later_server_t* s);
+/* Largest number of budget bytes held at once since the server was created. */
+int64_t later_c_ls_server_hbm_peak(later_server_t* s);
 /* Drains the queue, joins the workers and frees the budget. */
 void later_c_ls_server_destroy(later_server_t* s);
 

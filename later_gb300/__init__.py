@@ -114,6 +114,7 @@ _SIGS = {
     "later_c_ls_server_submit": (_i64, [_vp, ctypes.POINTER(LsRequest)]),
     "later_c_ls_server_wait": (_i, [_vp, _i64, ctypes.POINTER(LsResult)]),
     "later_c_ls_server_hbm_in_use": (_i64, [_vp]),
+    "later_c_ls_server_hbm_peak": (_i64, [_vp]),
     "later_c_ls_server_destroy": (None, [_vp]),
     "later_c_launch_count": (ctypes.c_uint64, []),
     "later_c_trace_begin": (None, []),
@@ -447,6 +448,9 @@ class LsServer:
 
     def hbm_in_use(self):
         return int(lib().later_c_ls_server_hbm_in_use(self._h))
+
+    def hbm_peak(self):
+        return int(lib().later_c_ls_server_hbm_peak(self._h))
 
     def close(self):
         if self._h:

@@ -51,96 +51,274 @@ __device__ __forceinline__ void put16(void* hi, void* lo, int64_t o, float v, in
   }
 }
 
-// X L^T = B (right, lower, transposed), L nb x nb (nb <= 128), B m x nb. One
-// thread per row of B; L and the rows being solved live in shared memory.
-__global__ void __launch_bounds__(128) trsm_rlt_leaf(int m, int nb, const float* __restrict__ L, int64_t ldl,
+// Zeros `n` floats of shared memory (16-byte aligned, n a multiple of 4).
+__device__ __forceinline__ void zero_smem(float* p, int n) {
+  for (int e = threadIdx.x; e < n / 4; e += blockDim.x) reinterpret_cast<float4*>(p)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Copies the nb x nb lower triangle of column-major L (ld ldl) into shared
+// memory, element (i, j) at dst[i * si + j * sj]; zeros above the diagonal.
+// Global reads are coalesced (i fastest) and issued eight per thread before
+// the shared-memory stores, so the copy is not one memory latency per element.
+__device__ __forceinline__ void stage_lower(int nb, const float* L, int64_t ldl, float* dst, int si, int sj) {
+  const int total = nb * nb;
+  const int T = blockDim.x;
+  for (int base = threadIdx.x; base < total; base += 8 * T) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * T;
+      const int i = e % nb, j = e / nb;
+      v[u] = (e < total && j <= i) ? L[i + static_cast<int64_t>(j) * ldl] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * T;
+      if (e < total) dst[(e % nb) * si + (e / nb) * sj] = v[u];
+    }
+  }
+}
+
+// Copies columns 0..nb-1 (rows 0..nb-1) of column-major L into shared memory
+// column-major with stride `ldc` (a multiple of 4). float4 reads when L and ldl
+// allow it; eight reads in flight per thread before the stores.
+__device__ __forceinline__ void stage_cols(int nb, const float* L, int64_t ldl, float* dst, int ldc) {
+  const int T = blockDim.x;
+  const bool vec = (reinterpret_cast<uintptr_t>(L) % 16 == 0) && (ldl % 4 == 0) && (nb % 4 == 0);
+  if (vec) {
+    const int nq = nb / 4, total = nq * nb;
+    for (int base = threadIdx.x; base < total; base += 8 * T) {
+      float4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * T;
+        v[u] = e < total ? *reinterpret_cast<const float4*>(L + 4 * (e % nq) + static_cast<int64_t>(e / nq) * ldl)
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * T;
+        if (e < total) *reinterpret_cast<float4*>(dst + 4 * (e % nq) + (e / nq) * ldc) = v[u];
+      }
+    }
+  } else {
+    const int total = nb * nb;
+    for (int base = threadIdx.x; base < total; base += 8 * T) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * T;
+        v[u] = e < total ? L[e % nb + static_cast<int64_t>(e / nb) * ldl] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * T;
+        if (e < total) dst[e % nb + (e / nb) * ldc] = v[u];
+      }
+    }
+  }
+}
+
+// X L^T = B (right, lower, transposed), L nb x nb (nb <= 128), B m x nb.
+// One CTA (256 threads) per R rows of B (R = 32 or 64), all of it parallel
+// over rows and columns: the 32 x 32 diagonal blocks D_c of L are inverted
+// once per CTA (warp c, lane = column of the inverse, forward substitution),
+// then for each block column X_c = (B_c - X_<c L_c,<c^T) D_c^-T runs as two
+// small shared-memory GEMMs in 2 x 4 register tiles: the product with D_c^-T,
+// then the update of the columns after the block.
+constexpr int LDL = 132;  // shared-memory stride of staged L (16-byte aligned)
+constexpr int XS = 132;   // shared-memory row stride of the X tile
+__global__ void __launch_bounds__(256) trsm_rlt_leaf(int m, int nb, int R, const float* __restrict__ L, int64_t ldl,
                                                      float* B, int64_t ldb, void* xh, void* xl, int64_t ldh,
                                                      int mode) {
-  extern __shared__ float sm[];
-  float* Ls = sm;                // [nb][129]  Ls[j*129 + i] = L[j][i]
-  float* Xs = sm + NB * 129;     // [128 rows][129]
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int j = e % nb, i = e / nb;
-    Ls[j * 129 + i] = (i <= j) ? L[j + static_cast<int64_t>(i) * ldl] : 0.f;
+  extern __shared__ __align__(16) float sm[];
+  float* Lc = sm;             // L[j][l] at l*LDL + j; diagonal blocks replaced by their inverses
+  float* Xs = sm + LDL * NB;  // X[r][c] at r*XS + c
+  const int row0 = blockIdx.x * R;
+  stage_cols(nb, L, ldl, Lc, LDL);
+  {
+    const int total = R * nb;
+    for (int base = threadIdx.x; base < total; base += 8 * 256) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * 256;
+        const int r = e % R, c = e / R;
+        v[u] = (e < total && row0 + r < m) ? B[row0 + r + static_cast<int64_t>(c) * ldb] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * 256;
+        if (e < total) Xs[(e % R) * XS + e / R] = v[u];
+      }
+    }
   }
-  const int r0 = blockIdx.x * 128;
-  const int row = r0 + threadIdx.x;
-  const bool in = row < m;
-  for (int j = 0; j < nb; ++j) Xs[threadIdx.x * 129 + j] = in ? B[row + static_cast<int64_t>(j) * ldb] : 0.f;
   __syncthreads();
-  if (!in) return;
-  float* x = Xs + threadIdx.x * 129;
-  for (int j = 0; j < nb; ++j) {
-    float acc = x[j];
-    const float* lj = Ls + j * 129;
-    for (int i = 0; i < j; ++i) acc -= x[i] * lj[i];
-    acc /= lj[j];
-    x[j] = acc;
-    B[row + static_cast<int64_t>(j) * ldb] = acc;
-    put16(xh, xl, row + static_cast<int64_t>(j) * ldh, acc, mode);
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  const int nblk = (nb + 31) / 32;
+  {
+    float y[32];
+    const int cb = warp * 32, w = min(32, nb - cb);
+    if (warp < nblk) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i) y[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        if (k < w) {
+          const float* dcol = Lc + (cb + k) * LDL + cb;  // column k of D
+          y[k] = y[k] / dcol[k];
+#pragma unroll
+          for (int i = k + 1; i < 32; ++i) y[i] -= dcol[i] * y[k];
+        }
+      }
+    }
+    __syncthreads();  // every read of the diagonal blocks is done
+    if (warp < nblk && lane < w) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        if (i < w) Lc[(cb + lane) * LDL + cb + i] = y[i];  // column `lane` of D^-1, zeros above the diagonal
+    }
+  }
+  __syncthreads();
+  for (int cb = 0; cb < nb; cb += 32) {
+    const int w = min(32, nb - cb);
+    // X_c <- X_c D_c^-T: out(r, j) = sum_i X[r][cb + i] Dinv[j][i]
+    const bool act = threadIdx.x < (R / 2) * 8;
+    const int ra = 2 * (threadIdx.x / 8), ja = 4 * (threadIdx.x % 8);
+    float acc[2][4] = {};
+    if (act) {
+#pragma unroll 4
+      for (int i = 0; i < w; ++i) {
+        const float4 d = *reinterpret_cast<const float4*>(&Lc[(cb + i) * LDL + cb + ja]);
+        const float x0 = Xs[ra * XS + cb + i], x1 = Xs[(ra + 1) * XS + cb + i];
+        acc[0][0] += x0 * d.x; acc[0][1] += x0 * d.y; acc[0][2] += x0 * d.z; acc[0][3] += x0 * d.w;
+        acc[1][0] += x1 * d.x; acc[1][1] += x1 * d.y; acc[1][2] += x1 * d.z; acc[1][3] += x1 * d.w;
+      }
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int row = row0 + ra + u;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int j = ja + v;
+          if (j < w) {
+            Xs[(ra + u) * XS + cb + j] = acc[u][v];
+            if (row < m) {
+              const int64_t o = static_cast<int64_t>(cb + j);
+              B[row + o * ldb] = acc[u][v];
+              put16(xh, xl, row + o * ldh, acc[u][v], mode);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // columns after the block: X[r][jj] -= sum_l X[r][cb + l] L[jj][cb + l]
+    const int c1 = cb + w, W = nb - c1;
+    if (W > 0) {
+      const int nq = (W + 3) / 4, ntile = (R / 2) * nq;
+      for (int q = threadIdx.x; q < ntile; q += 256) {
+        const int r = 2 * (q / nq), jj = c1 + 4 * (q % nq);
+        float a[2][4] = {};
+#pragma unroll 8
+        for (int l = 0; l < 32; ++l) {
+          const float4 v = *reinterpret_cast<const float4*>(&Lc[(cb + l) * LDL + jj]);
+          const float x0 = Xs[r * XS + cb + l], x1 = Xs[(r + 1) * XS + cb + l];
+          a[0][0] += x0 * v.x; a[0][1] += x0 * v.y; a[0][2] += x0 * v.z; a[0][3] += x0 * v.w;
+          a[1][0] += x1 * v.x; a[1][1] += x1 * v.y; a[1][2] += x1 * v.z; a[1][3] += x1 * v.w;
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+            if (jj + v < nb) Xs[(r + u) * XS + jj + v] -= a[u][v];
+      }
+    }
+    __syncthreads();
   }
 }
 
 // L X = B (left, lower, no transpose), L nb x nb (nb <= 128), B nb x n. One
-// CTA per 32 columns of B staged in shared memory; one thread per column.
-__global__ void __launch_bounds__(32) trsm_lln_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl, float* B,
-                                                    int64_t ldb, void* xh, void* xl, int64_t ldh, int mode) {
-  extern __shared__ float sm[];
-  float* Ls = sm;             // [i][k] at i*129 + k
-  float* Bs = sm + NB * 129;  // [col][row] at c*129 + r
-  const int c0 = blockIdx.x * 32;
-  for (int e = threadIdx.x; e < nb * nb; e += 32) {
-    const int i = e % nb, k = e / nb;
-    Ls[i * 129 + k] = (k <= i) ? L[i + static_cast<int64_t>(k) * ldl] : 0.f;
-  }
-  for (int c = 0; c < 32; ++c)
-    for (int r = threadIdx.x; r < nb; r += 32)
-      Bs[c * 129 + r] = (c0 + c < n) ? B[r + static_cast<int64_t>(c0 + c) * ldb] : 0.f;
+// warp per column of B, eight columns per CTA; lane l holds rows l, l+32,
+// l+64, l+96. Right-looking: x_k is broadcast from its owner lane and every
+// lane updates its rows below k. L is staged column-major (stride 129).
+__global__ void __launch_bounds__(256) trsm_lln_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl, float* B,
+                                                     int64_t ldb, void* xh, void* xl, int64_t ldh, int mode) {
+  extern __shared__ __align__(16) float sm[];
+  float* Lc = sm;  // L[i][k] at i + k*129
+  stage_lower(nb, L, ldl, Lc, 1, 129);
   __syncthreads();
-  float* x = Bs + threadIdx.x * 129;
-  for (int i = 0; i < nb; ++i) {
-    float acc = x[i];
-    const float* li = Ls + i * 129;
-    for (int k = 0; k < i; ++k) acc -= li[k] * x[k];
-    x[i] = acc / li[i];
+  const int lane = threadIdx.x % 32;
+  const int c = blockIdx.x * 8 + threadIdx.x / 32;
+  if (c >= n) return;
+  float b[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = lane + 32 * q;
+    b[q] = r < nb ? B[r + static_cast<int64_t>(c) * ldb] : 0.f;
   }
-  __syncthreads();
-  for (int c = 0; c < 32; ++c) {
-    if (c0 + c >= n) break;
-    for (int r = threadIdx.x; r < nb; r += 32) {
-      const float v = Bs[c * 129 + r];
-      B[r + static_cast<int64_t>(c0 + c) * ldb] = v;
-      put16(xh, xl, r + static_cast<int64_t>(c0 + c) * ldh, v, mode);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    for (int kk = 0; kk < 32; ++kk) {
+      const int k = 32 * q + kk;
+      if (k >= nb) break;
+      const float xk = __shfl_sync(0xffffffffu, b[q], kk) / Lc[k + k * 129];
+      if (lane == kk) b[q] = xk;
+#pragma unroll
+      for (int q2 = q; q2 < 4; ++q2) {
+        const int r = lane + 32 * q2;
+        if (r > k && r < nb) b[q2] -= Lc[r + k * 129] * xk;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = lane + 32 * q;
+    if (r < nb) {
+      B[r + static_cast<int64_t>(c) * ldb] = b[q];
+      put16(xh, xl, r + static_cast<int64_t>(c) * ldh, b[q], mode);
     }
   }
 }
 
 // L^T X = B (left, lower, transposed), L nb x nb (nb <= 128), B nb x n:
-// backward substitution, one thread per column of B staged in shared memory.
-__global__ void __launch_bounds__(32) trsm_llt_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl, float* B,
-                                                    int64_t ldb) {
-  extern __shared__ float sm[];
-  float* Ls = sm;             // [k][i] at k*129 + i  (= L[k][i])
-  float* Bs = sm + NB * 129;  // [col][row]
-  const int c0 = blockIdx.x * 32;
-  for (int e = threadIdx.x; e < nb * nb; e += 32) {
-    const int k = e % nb, i = e / nb;
-    Ls[k * 129 + i] = (k >= i) ? L[k + static_cast<int64_t>(i) * ldl] : 0.f;
-  }
-  for (int c = 0; c < 32; ++c)
-    for (int r = threadIdx.x; r < nb; r += 32)
-      Bs[c * 129 + r] = (c0 + c < n) ? B[r + static_cast<int64_t>(c0 + c) * ldb] : 0.f;
+// backward substitution, one warp per column as above; L is staged row-major
+// (stride 129) so that row k of L, which multiplies x_k, is contiguous.
+__global__ void __launch_bounds__(256) trsm_llt_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl, float* B,
+                                                     int64_t ldb) {
+  extern __shared__ __align__(16) float sm[];
+  float* Lr = sm;  // L[k][i] at k*129 + i
+  stage_lower(nb, L, ldl, Lr, 129, 1);
   __syncthreads();
-  float* x = Bs + threadIdx.x * 129;
-  for (int i = nb - 1; i >= 0; --i) {
-    float acc = x[i];
-    for (int k = i + 1; k < nb; ++k) acc -= Ls[k * 129 + i] * x[k];
-    x[i] = acc / Ls[i * 129 + i];
+  const int lane = threadIdx.x % 32;
+  const int c = blockIdx.x * 8 + threadIdx.x / 32;
+  if (c >= n) return;
+  float b[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = lane + 32 * q;
+    b[q] = r < nb ? B[r + static_cast<int64_t>(c) * ldb] : 0.f;
   }
-  __syncthreads();
-  for (int c = 0; c < 32; ++c) {
-    if (c0 + c >= n) break;
-    for (int r = threadIdx.x; r < nb; r += 32) B[r + static_cast<int64_t>(c0 + c) * ldb] = Bs[c * 129 + r];
+#pragma unroll
+  for (int q = 3; q >= 0; --q) {
+    for (int kk = 31; kk >= 0; --kk) {
+      const int k = 32 * q + kk;
+      if (k >= nb) continue;
+      const float xk = __shfl_sync(0xffffffffu, b[q], kk) / Lr[k * 129 + k];
+      if (lane == kk) b[q] = xk;
+#pragma unroll
+      for (int q2 = 0; q2 <= q; ++q2) {
+        const int r = lane + 32 * q2;
+        if (r < k) b[q2] -= Lr[k * 129 + r] * xk;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = lane + 32 * q;
+    if (r < nb) B[r + static_cast<int64_t>(c) * ldb] = b[q];
   }
 }
 
@@ -152,13 +330,20 @@ __global__ void __launch_bounds__(256) trmm_leaf(int nb, int n, const float* __r
   float* Ls = sm;             // [i][k]
   float* Bs = sm + NB * 129;  // [k][c] at k*65 + c
   const int c0 = blockIdx.x * 64;
-  for (int e = threadIdx.x; e < nb * nb; e += 256) {
-    const int i = e % nb, k = e / nb;
-    Ls[i * 129 + k] = (k <= i) ? L[i + static_cast<int64_t>(k) * ldl] : 0.f;
-  }
-  for (int e = threadIdx.x; e < nb * 64; e += 256) {
-    const int k = e % nb, c = e / nb;
-    Bs[k * 65 + c] = (c0 + c < n) ? B[k + static_cast<int64_t>(c0 + c) * ldb] : 0.f;
+  stage_lower(nb, L, ldl, Ls, 129, 1);
+  for (int base = threadIdx.x; base < nb * 64; base += 8 * 256) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + 256 * u;
+      const int k = e % nb, c = e / nb;
+      v[u] = (e < nb * 64 && c0 + c < n) ? B[k + static_cast<int64_t>(c0 + c) * ldb] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + 256 * u;
+      if (e < nb * 64) Bs[(e % nb) * 65 + e / nb] = v[u];
+    }
   }
   __syncthreads();
   for (int e = threadIdx.x; e < nb * 64; e += 256) {
@@ -170,42 +355,123 @@ __global__ void __launch_bounds__(256) trmm_leaf(int nb, int n, const float* __r
   }
 }
 
-// Lower Cholesky of an nb x nb block (nb <= 128) in one CTA, in shared memory.
-// Right-looking; a non-positive (or NaN) pivot sets DEV_NUMERIC and the
-// factorisation continues with pivot 1 so the kernel always finishes.
-__global__ void __launch_bounds__(1024) potrf_leaf(int nb, float* A, int64_t lda, int* status) {
-  extern __shared__ float sm[];
-  float* As = sm;  // [i][j] at i*129 + j (lower part used)
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int i = e % nb, j = e / nb;
-    if (i >= j) As[i * 129 + j] = A[i + static_cast<int64_t>(j) * lda];
-  }
-  __shared__ float piv;
+// Lower Cholesky of an nb x nb block (nb <= 128) in one CTA, in shared memory
+// (column-major, stride LDL), right-looking over 32-column blocks. Warp 0
+// factors the 32 x 32 diagonal block with lane = row in registers: per pivot
+// one IEEE square root and one reciprocal (the column is scaled by it, as
+// LAPACK's spotf2 does), the scaled column broadcast through shared memory as
+// float4. One thread per row then solves the block column below the diagonal
+// block, and the CTA updates the trailing lower triangle in 4 x 4 register
+// tiles. A non-positive (or NaN) pivot sets DEV_NUMERIC and the factorisation
+// continues with pivot 1 so the kernel always finishes.
+__global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda, int* status) {
+  extern __shared__ __align__(16) float sm[];
+  float* Ac = sm;                // A[i][j] at j*LDL + i (lower triangle used)
+  float* col = sm + LDL * NB;    // 32 floats: broadcast column
+  float* rdiag = col + 32;       // 32 floats: reciprocals of the block's pivots
+  stage_cols(nb, A, lda, Ac, LDL);
   __syncthreads();
-  for (int k = 0; k < nb; ++k) {
-    if (threadIdx.x == 0) {
-      float d = As[k * 129 + k];
-      if (!(d > 0.f)) {
-        report(status, DEV_NUMERIC);
-        d = 1.f;
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  for (int k0 = 0; k0 < nb; k0 += 32) {
+    const int kb = min(32, nb - k0);
+    if (warp == 0) {
+      float d[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) d[j] = (lane < kb && j <= lane) ? Ac[(k0 + j) * LDL + k0 + lane] : 0.f;
+      bool bad = false;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        if (k < kb) {
+          float dk = __shfl_sync(0xffffffffu, d[k], k);
+          if (!(dk > 0.f)) {
+            bad = true;
+            dk = 1.f;
+          }
+          const float piv = sqrtf(dk);
+          const float rinv = 1.f / piv;
+          if (lane == k) {
+            d[k] = piv;
+            rdiag[k] = rinv;
+          }
+          if (lane > k) d[k] *= rinv;
+          col[lane] = d[k];
+          __syncwarp();
+#pragma unroll
+          for (int jq = (k + 1) / 4; jq < 8; ++jq) {
+            const float4 c4 = reinterpret_cast<const float4*>(col)[jq];
+            const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int j = 4 * jq + e;
+              if (j > k && lane >= j) d[j] -= d[k] * cv[e];
+            }
+          }
+          __syncwarp();
+        }
       }
-      piv = sqrtf(d);
-      As[k * 129 + k] = piv;
+      if (bad && lane == 0) report(status, DEV_NUMERIC);
+      if (lane < kb) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (j <= lane) Ac[(k0 + j) * LDL + k0 + lane] = d[j];
+      }
     }
     __syncthreads();
-    const float inv = 1.f / piv;
-    for (int i = k + 1 + threadIdx.x; i < nb; i += blockDim.x) As[i * 129 + k] *= inv;
+    // rows below the diagonal block: x D^T = a (D = L[k0.., k0..], kb x kb)
+    const int t0 = k0 + kb;
+    for (int r = t0 + threadIdx.x; r < nb; r += blockDim.x) {
+      float x[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] = j < kb ? Ac[(k0 + j) * LDL + r] : 0.f;
+#pragma unroll
+      for (int l = 0; l < 32; ++l) {
+        if (l < kb) {
+          x[l] *= rdiag[l];
+          const float* dcol = Ac + (k0 + l) * LDL + k0;  // column l of D
+#pragma unroll
+          for (int j = l + 1; j < 32; ++j) x[j] -= x[l] * dcol[j];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (j < kb) Ac[(k0 + j) * LDL + r] = x[j];
+    }
     __syncthreads();
-    const int t = nb - k - 1;  // trailing size; update the lower triangle of it
-    for (int e = threadIdx.x; e < t * t; e += blockDim.x) {
-      const int i = k + 1 + e % t, j = k + 1 + e / t;
-      if (i >= j) As[i * 129 + j] -= As[i * 129 + k] * As[j * 129 + k];
+    // trailing lower triangle: A[i][j] -= sum_l A[i][k0+l] A[j][k0+l], i >= j >= t0
+    const int t = nb - t0;
+    const int nt = (t + 3) / 4;
+    const int ntiles = nt * (nt + 1) / 2;
+    for (int q = threadIdx.x; q < ntiles; q += blockDim.x) {
+      int ti = static_cast<int>((sqrtf(8.f * q + 1.f) - 1.f) * 0.5f);
+      while (ti * (ti + 1) / 2 > q) --ti;
+      while ((ti + 1) * (ti + 2) / 2 <= q) ++ti;
+      const int tj = q - ti * (ti + 1) / 2;
+      const int i0 = t0 + 4 * ti, j0 = t0 + 4 * tj;
+      float acc[4][4] = {};
+#pragma unroll 8
+      for (int l = 0; l < 32; ++l) {
+        const float4 a = *reinterpret_cast<const float4*>(&Ac[(k0 + l) * LDL + i0]);
+        const float4 b = *reinterpret_cast<const float4*>(&Ac[(k0 + l) * LDL + j0]);
+        const float av[4] = {a.x, a.y, a.z, a.w};
+        const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] += av[u] * bv[v];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int i = i0 + u, j = j0 + v;
+          if (i < nb && j <= i) Ac[j * LDL + i] -= acc[u][v];
+        }
     }
     __syncthreads();
   }
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int i = e % nb, j = e / nb;
-    if (i >= j) A[i + static_cast<int64_t>(j) * lda] = As[i * 129 + j];
+    if (i >= j) A[i + static_cast<int64_t>(j) * lda] = Ac[j * LDL + i];
   }
 }
 
@@ -298,10 +564,12 @@ later_status_t gemm(B3& b, char ta, char tb, int M, int N, int K, float alpha, c
 later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float* B, int64_t ldb, char* xh, char* xl,
                         int64_t ldh, int fp32_lim = kFp32Trsm) {
   if (n <= NB) {
-    const size_t smem = (NB * 129 + 128 * 129) * sizeof(float);
+    const size_t smem = (LDL * NB + 64 * XS) * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(trsm_rlt_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_OTHER);
-    trsm_rlt_leaf<<<(m + 127) / 128, 128, smem, b.st>>>(m, n, L, ldl, B, ldb, xh, xl, ldh, mode_of(b.o.prec));
+    // 64 rows per CTA while that still gives two CTAs per SM, else 32
+    const int R = (m + 63) / 64 >= 2 * num_sms() ? 64 : 32;
+    trsm_rlt_leaf<<<(m + R - 1) / R, 256, smem, b.st>>>(m, n, R, L, ldl, B, ldb, xh, xl, ldh, mode_of(b.o.prec));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -328,10 +596,10 @@ later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float*
 later_status_t trsm_lln(B3& b, int m, int n, const float* L, int64_t ldl, float* B, int64_t ldb, char* xh, char* xl,
                         int64_t ldh, int fp32_lim = kFp32Trsm) {
   if (m <= NB) {
-    const size_t smem = (NB * 129 + 32 * 129) * sizeof(float);
+    const size_t smem = NB * 129 * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(trsm_lln_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_OTHER);
-    trsm_lln_leaf<<<(n + 31) / 32, 32, smem, b.st>>>(m, n, L, ldl, B, ldb, xh, xl, ldh, mode_of(b.o.prec));
+    trsm_lln_leaf<<<(n + 7) / 8, 256, smem, b.st>>>(m, n, L, ldl, B, ldb, xh, xl, ldh, mode_of(b.o.prec));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -359,10 +627,10 @@ later_status_t trsm_lln(B3& b, int m, int n, const float* L, int64_t ldl, float*
 later_status_t trsm_llt(B3& b, int m, int n, const float* L, int64_t ldl, float* B, int64_t ldb,
                         int fp32_lim = kFp32Trsm) {
   if (m <= NB) {
-    const size_t smem = (NB * 129 + 32 * 129) * sizeof(float);
+    const size_t smem = NB * 129 * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(trsm_llt_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_OTHER);
-    trsm_llt_leaf<<<(n + 31) / 32, 32, smem, b.st>>>(m, n, L, ldl, B, ldb);
+    trsm_llt_leaf<<<(n + 7) / 8, 256, smem, b.st>>>(m, n, L, ldl, B, ldb);
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -416,10 +684,10 @@ later_status_t trmm_rec(B3& b, int m, int n, const float* L, int64_t ldl, const 
 
 later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda) {
   if (n <= NB) {
-    const size_t smem = NB * 129 * sizeof(float);
+    const size_t smem = (NB * LDL + 64) * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(potrf_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_PANEL);
-    potrf_leaf<<<1, 1024, smem, b.st>>>(n, A, lda, device_status_ptr());
+    potrf_leaf<<<1, 256, smem, b.st>>>(n, A, lda, device_status_ptr());
     note_launch();
     return cuda_status(cudaGetLastError());
   }

@@ -363,72 +363,70 @@ __global__ void __launch_bounds__(256) tn_reduce_kernel(int nch, int ntiles, int
   *o = accumulate ? *o + alpha * s : alpha * s;
 }
 
-// Y[rows, cols] -= X[rows, :] * S[:, cols] with S (k1 x k2). One CTA per 64
-// rows x 64 columns; the inner dimension is walked in chunks of 64 with X and
-// S staged in shared memory; each thread updates 4 rows x 4 columns. Optional
-// 16-bit copy of the updated Y (mode 0 fp16, 1 bf16, 2 split3 hi/lo).
+// Y[rows, cols] += alpha X[rows, :] S[:, cols] with S (k1 x k2; stored
+// transposed when s_trans). One CTA per 64 rows x 64 columns; the inner
+// dimension is walked in chunks of 64 with X and alpha*S staged k-major in
+// shared memory; each thread accumulates 4 consecutive rows x 4 consecutive
+// columns from float4 reads, and adds the sum into Y once at the end.
+// Optional 16-bit copy of the updated Y (mode 0 fp16, 1 bf16, 2 split3 hi/lo).
 constexpr int NNR = 64;
 __global__ void __launch_bounds__(256) nn_update_kernel(int m, int k1, int k2, float alpha, const float* __restrict__ X,
                                                         int64_t ldx, const float* __restrict__ S, int64_t lds,
                                                         int s_trans, int lower, float* __restrict__ Y, int64_t ldy,
                                                         void* yh, void* yl, int64_t ldh, int mode) {
-  __shared__ float Ss[64][65];
-  __shared__ float Xs[NNR][65];
+  __shared__ __align__(16) float Ss[64][68];  // [k][col]
+  __shared__ __align__(16) float Xs[64][68];  // [k][row]
   const int r0 = blockIdx.x * NNR;
   const int c0 = blockIdx.y * 64;
   if (lower && r0 + NNR - 1 < c0) return;  // tile entirely above the diagonal
   const int mm = min(NNR, m - r0);
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // rows tx + 16 a, cols ty + 16 b
-  float y[4][4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int i = tx + 16 * u, j = c0 + ty + 16 * v;
-      y[u][v] = (i < mm && j < k2) ? __ldcg(&Y[r0 + i + static_cast<int64_t>(j) * ldy]) : 0.f;
-    }
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;  // rows 4 tx + u, cols 4 ty + v
+  float acc[4][4] = {};
   for (int k0 = 0; k0 < k1; k0 += 64) {
     float sv[16], xv[16];
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
       const int e = threadIdx.x + 256 * u;
-      const int i = e % 64, j = e / 64;
-      const bool ins = (k0 + i < k1 && c0 + j < k2);
-      sv[u] = !ins ? 0.f
-                   : (s_trans ? S[c0 + j + static_cast<int64_t>(k0 + i) * lds]
-                              : S[k0 + i + static_cast<int64_t>(c0 + j) * lds]);
-      xv[u] = (i < mm && k0 + j < k1) ? __ldcg(&X[r0 + i + static_cast<int64_t>(k0 + j) * ldx]) : 0.f;
+      const int lo = e % 64, hi = e / 64;
+      xv[u] = (lo < mm && k0 + hi < k1) ? __ldcg(&X[r0 + lo + static_cast<int64_t>(k0 + hi) * ldx]) : 0.f;
+      if (s_trans)  // S[c][k] at c + k lds: lo = column, hi = k
+        sv[u] = (c0 + lo < k2 && k0 + hi < k1) ? S[c0 + lo + static_cast<int64_t>(k0 + hi) * lds] : 0.f;
+      else          // S[k][c] at k + c lds: lo = k, hi = column
+        sv[u] = (k0 + lo < k1 && c0 + hi < k2) ? S[k0 + lo + static_cast<int64_t>(c0 + hi) * lds] : 0.f;
     }
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
       const int e = threadIdx.x + 256 * u;
-      Ss[e % 64][e / 64] = sv[u];
-      Xs[e % 64][e / 64] = xv[u];
+      const int lo = e % 64, hi = e / 64;
+      Xs[hi][lo] = xv[u];
+      if (s_trans)
+        Ss[hi][lo] = alpha * sv[u];
+      else
+        Ss[lo][hi] = alpha * sv[u];
     }
     __syncthreads();
 #pragma unroll 8
     for (int k = 0; k < 64; ++k) {
-      float xr[4], sr[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        xr[u] = Xs[tx + 16 * u][k];
-        sr[u] = Ss[k][ty + 16 * u];
-      }
+      const float4 xr = *reinterpret_cast<const float4*>(&Xs[k][4 * tx]);
+      const float4 sr = *reinterpret_cast<const float4*>(&Ss[k][4 * ty]);
+      const float xa[4] = {xr.x, xr.y, xr.z, xr.w};
+      const float sa[4] = {sr.x, sr.y, sr.z, sr.w};
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) y[u][v] += alpha * (xr[u] * sr[v]);
+        for (int v = 0; v < 4; ++v) acc[u][v] += xa[u] * sa[v];
     }
   }
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const int i = tx + 16 * u, j = c0 + ty + 16 * v;
+      const int i = 4 * tx + u, j = c0 + 4 * ty + v;
       if (i < mm && j < k2 && (!lower || r0 + i >= j)) {
-        const float val = y[u][v];
-        Y[r0 + i + static_cast<int64_t>(j) * ldy] = val;
+        float* yp = &Y[r0 + i + static_cast<int64_t>(j) * ldy];
+        const float val = *yp + acc[u][v];
+        *yp = val;
         if (yh) {
           const int64_t o = r0 + i + static_cast<int64_t>(j) * ldh;
           if (mode == 1) {

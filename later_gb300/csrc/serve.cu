@@ -50,6 +50,7 @@ class HbmPool {
         free_.erase(it);
         if (rest) free_[off + bytes] = rest;
         used_ += bytes;
+        if (used_ > peak_) peak_ = used_;
         return off;
       }
     }
@@ -73,11 +74,13 @@ class HbmPool {
     }
   }
   size_t used() const { return used_; }
+  size_t peak() const { return peak_; }
   size_t size() const { return size_; }
 
  private:
   size_t size_;
   size_t used_ = 0;
+  size_t peak_ = 0;
   std::map<size_t, size_t> free_;
 };
 
@@ -278,6 +281,12 @@ int64_t later_c_ls_server_hbm_in_use(later_server_t* s) {
   if (!s) return 0;
   std::lock_guard<std::mutex> lk(s->mu);
   return static_cast<int64_t>(s->pool->used());
+}
+
+int64_t later_c_ls_server_hbm_peak(later_server_t* s) {
+  if (!s) return 0;
+  std::lock_guard<std::mutex> lk(s->mu);
+  return static_cast<int64_t>(s->pool->peak());
 }
 
 void later_c_ls_server_destroy(later_server_t* s) {

@@ -1,6 +1,4 @@
 """Least-squares serving loop: continuous batching under an HBM budget."""
-import threading
-import time
 
 import numpy as np
 import pytest
@@ -52,22 +50,12 @@ def test_admission_respects_the_hbm_budget(cuda):
     reqs = _requests(6, seed=2, mmax=4096, nmax=256)
     budget_gb = 0.2
     srv = lg.LsServer(slots=4, hbm_budget_gb=budget_gb)
-    peak = [0]
-    stop = threading.Event()
-
-    def poll():
-        while not stop.is_set():
-            peak[0] = max(peak[0], srv.hbm_in_use())
-            time.sleep(0.0005)
-
-    th = threading.Thread(target=poll)
-    th.start()
     tickets = [srv.submit(A, B) for A, B in reqs]
     outs = [srv.wait(t) for t in tickets]
-    stop.set()
-    th.join()
     assert all(r["status"] == 0 for _, r in outs)
-    assert 0 < peak[0] <= budget_gb * (1 << 30)
+    # the pool's own high-water mark: something was admitted, never beyond the budget
+    assert 0 < srv.hbm_peak() <= budget_gb * (1 << 30)
+    assert srv.hbm_in_use() == 0
     # A request larger than the whole budget is refused up front.
     big = gen.normal(16384, 1024, seed=3)
     with pytest.raises(lg.LaterError) as e:
