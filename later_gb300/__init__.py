@@ -39,12 +39,13 @@ class LaterError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("cgs2", ctypes.c_int), ("leaf", ctypes.c_int),
-                ("reserved", ctypes.c_int), ("timeout_cycles", ctypes.c_longlong)]
+                ("panel", ctypes.c_int), ("timeout_cycles", ctypes.c_longlong)]
 
     @classmethod
-    def make(cls, precision="fp16", cgs2=False, leaf=128, timeout_cycles=0) -> "Options":
+    def make(cls, precision="fp16", cgs2=False, leaf=128, timeout_cycles=0, panel=0) -> "Options":
         p = PREC[precision] if isinstance(precision, str) else int(precision)
-        return cls(p, int(bool(cgs2)), int(leaf), 0, int(timeout_cycles))
+        pn = {"fused": 0, "mgs": 1}[panel] if isinstance(panel, str) else int(panel)
+        return cls(p, int(bool(cgs2)), int(leaf), pn, int(timeout_cycles))
 
 
 class SolveInfo(ctypes.Structure):
@@ -202,7 +203,7 @@ def rgsqrf_bufsize(m, n, precision="fp16", cgs2=False, leaf=128):
 
 
 def later_rgsqrf(A, R=None, work=None, hwork=None, *, precision="fp16", cgs2=False, leaf=128, timeout_cycles=0,
-                 stream=None):
+                 stream=None, panel="fused"):
     """Recursive Gram-Schmidt QR in place: A (m x n, column-major FP32 CUDA) becomes Q; returns R.
 
     Mirrors LATER's `later_rgsqrf(ctxt, m, n, A, lda, R, ldr, work, lwork, hwork, lhwork)`
@@ -219,7 +220,7 @@ def later_rgsqrf(A, R=None, work=None, hwork=None, *, precision="fp16", cgs2=Fal
         work = torch.empty(lw, dtype=torch.float32, device=A.device)
     if hwork is None:
         hwork = torch.empty(lh, dtype=torch.float16, device=A.device)
-    o = Options.make(precision, cgs2, leaf, timeout_cycles)
+    o = Options.make(precision, cgs2, leaf, timeout_cycles, panel)
     _check(lib().later_c_rgsqrf(_stream(stream), m, n, A.data_ptr(), lda, R.data_ptr(), ldr, work.data_ptr(),
                                 work.numel(), hwork.data_ptr(), hwork.numel(), ctypes.byref(o)), "later_rgsqrf")
     return R

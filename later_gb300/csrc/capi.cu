@@ -17,7 +17,7 @@ void later_c_default_options(later_options_t* opt) {
   opt->precision = LATER_PREC_FP16;
   opt->cgs2 = 0;
   opt->leaf = 128;
-  opt->reserved = 0;
+  opt->panel = 0;
   opt->timeout_cycles = 0;
 }
 

@@ -1,0 +1,1124 @@
+// Fused rgsqrf leaf: one cooperative launch factors an m x w leaf (w <= 128).
+//
+// The reference's 128-wide leaf (mgs_caqr_panel_256x128, QR/panel.cu:10-63)
+// is four 32-column MGS-TSQR panels glued by six FP32 block-CGS GEMMs, each a
+// separate launch, and the panel tree itself is a chain of launches. On GB300
+// each of those steps is latency-bound (a 16384 x 32 panel is 2 MB: under a
+// microsecond of HBM time), so here the whole leaf is one persistent kernel:
+// every CTA owns a fixed slab of rows for the whole leaf and the CTAs meet
+// only at grid barriers around deterministic reductions.
+//
+//   panel (c0, k <= 32), CholQR2:
+//     G  = A^T A            slab partials -> barrier -> distributed reduction -> barrier
+//     R1 = chol(G)          every CTA, redundantly (bitwise identical)
+//     Q1 = A R1^-1          row-wise substitution, into scratch; G2 = Q1^T Q1 partials
+//     R2 = chol(G2)         (after the same reduction)
+//     Q  = Q1 R2^-1, R = R2 R1
+//   The panel falls back to MGS-TSQR (the reference's algorithm, the tree of
+//   tsqr_dev.cuh run over virtual blocks) when chol(G) meets a non-positive
+//   pivot or max|G2 - I| > 1/4; every CTA takes the same decision from the
+//   same numbers, and A is not written before it.
+//   update (Q cols [c0, c0+w1), A2 cols [c1, c1+w2)):
+//     P = Q^T A2 (partials -> reduction, also written into R), A2 -= Q P.
+//
+// Determinism: the row slabs depend only on m and the grid size; every
+// reduction sums the per-CTA partials in CTA order (lane-strided, then a fixed
+// shuffle tree), so results are reproducible run to run.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "leaf.cuh"
+#include "tsqr_dev.cuh"
+
+namespace later {
+namespace {
+
+constexpr int LT = 256;     // threads per CTA
+constexpr int GT = 256;     // rows per Gram / substitution tile (one per thread)
+constexpr int UT = 64;      // rows per update tile
+constexpr int SP = 68;      // row stride of the update tiles (16-byte rows)
+constexpr int PART = 4096;  // floats per CTA partial (64 x 64)
+constexpr int kMaxSteps = 8;
+constexpr int RCS = 36;  // stride of the column-major R factors in shared memory (16-byte columns)
+
+struct LeafStep {
+  int kind;  // 0: panel (c0, w1 columns); 1: update
+  int c0, w1, c1, w2;
+};
+
+struct LeafPlan {
+  int m, w, rpc, nsteps, cgs2, mode, vec;
+  LeafStep step[kMaxSteps];
+  float* A;
+  int64_t lda;
+  float* R;
+  int64_t ldr;
+  char* qh;
+  char* ql;
+  int64_t ldh;
+  float* q1;    // m x 32, ld m
+  float* part;  // gridDim.x x PART
+  float* red;   // PART
+  int* sync;    // arrive, exit, abort
+  TsqrPlan tsqr;
+  int* status;
+  long long budget;
+  int* fallbacks;
+};
+
+struct PanelSmem {
+  float S[32 * (GT + 1)];  // tile of 32 columns x GT rows (column c at c * (GT + 1))
+  float G[32 * 33];
+  float R1[32 * RCS];  // column-major factors
+  float R2[32 * RCS];
+  float rinv1[32];
+  float rinv2[32];
+  int ok;
+};
+
+struct UpdateSmem {
+  float Qs[UT * SP];
+  float As[UT * SP];
+  float Ps[64 * SP];
+};
+
+union LeafSmem {
+  PanelSmem p;
+  UpdateSmem u;
+  TsqrReduceSmem tr;
+  TsqrApplySmem ta;
+};
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier over the co-resident CTAs of a cooperative launch.
+// Monotonic arrival counter; every wait is bounded: on timeout the status word
+// gets DEV_TIMEOUT, the abort flag is raised and every CTA returns false.
+struct GridSync {
+  int* arrive;
+  int* abort;
+  int* status;
+  long long budget;
+  int epoch;
+};
+
+__device__ bool grid_barrier(GridSync& g, int* okflag) {
+  __syncthreads();
+  ++g.epoch;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(g.arrive, 1);
+    const int target = g.epoch * static_cast<int>(gridDim.x);
+    const long long t0 = clock64();
+    int good = 1;
+    while (ld_acquire(g.arrive) < target) {
+      if (ld_acquire(g.abort)) {
+        good = 0;
+        break;
+      }
+      if (clock64() - t0 > g.budget) {
+        report(g.status, DEV_TIMEOUT);
+        atomicExch(g.abort, 1);
+        good = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    *okflag = good;
+  }
+  __syncthreads();
+  return *okflag != 0;
+}
+
+// Copies `total` elements with eight global loads in flight per thread before
+// the shared-memory stores (ld(e) -> value, st(e, value)).
+template <class Ld, class St>
+__device__ __forceinline__ void batched_copy(int total, Ld ld, St st) {
+  for (int base = threadIdx.x; base < total; base += 8 * LT) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * LT;
+      v[u] = e < total ? ld(e) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * LT;
+      if (e < total) st(e, v[u]);
+    }
+  }
+}
+
+// Deterministic reduction of the per-CTA partials over the entries i < ni,
+// j < nj (entry i + ld j of every CTA's partial): the entries are split in
+// contiguous chunks over the CTAs; a CTA takes 32 entries at a time, one per
+// lane, warp w summing the partials of CTAs w, w + 8, ... (eight loads in
+// flight), and warp 0 adds the eight warp sums in a fixed order before
+// emit(entry, sum).
+template <class Emit>
+__device__ void reduce_partials(const float* part, int ni, int nj, int ld, Emit emit) {
+  __shared__ float ws[8][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int G = static_cast<int>(gridDim.x);
+  const int E = ni * nj;
+  const int per = (E + G - 1) / G;
+  const int e0 = blockIdx.x * per, e1 = min(E, e0 + per);
+  for (int base = e0; base < e1; base += 32) {
+    const int q = base + lane;
+    const bool has = q < e1;
+    const int e = has ? (q % ni) + ld * (q / ni) : 0;
+    float v[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int c = warp + 8 * t;
+      v[t] = (has && c < G) ? __ldcg(&part[static_cast<int64_t>(c) * PART + e]) : 0.f;
+    }
+    float sum = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
+    for (int c = warp + 64; c < G; c += 8) sum += has ? __ldcg(&part[static_cast<int64_t>(c) * PART + e]) : 0.f;
+    ws[warp][lane] = sum;
+    __syncthreads();
+    if (warp == 0 && has) {
+      const float t = ((ws[0][lane] + ws[1][lane]) + (ws[2][lane] + ws[3][lane])) +
+                      ((ws[4][lane] + ws[5][lane]) + (ws[6][lane] + ws[7][lane]));
+      emit(e, t);
+    }
+    __syncthreads();
+  }
+}
+
+// Gram partial of the tile in S (32 columns x GT rows): thread (ti, tj) adds
+// rows 2ti, 2ti+1 x columns 2tj, 2tj+1 of S^T S into acc.
+__device__ __forceinline__ void gram_tile(const float* S, int rows, float (&acc)[2][2]) {
+  const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+  const float* x0 = S + (2 * ti) * (GT + 1);
+  const float* x1 = x0 + (GT + 1);
+  const float* y0 = S + (2 * tj) * (GT + 1);
+  const float* y1 = y0 + (GT + 1);
+#pragma unroll 8
+  for (int r = 0; r < rows; ++r) {
+    const float a0 = x0[r], a1 = x1[r], b0 = y0[r], b1 = y1[r];
+    acc[0][0] += a0 * b0;
+    acc[0][1] += a0 * b1;
+    acc[1][0] += a1 * b0;
+    acc[1][1] += a1 * b1;
+  }
+}
+
+__device__ __forceinline__ void write_gram_partial(float* part, const float (&acc)[2][2]) {
+  const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+  float* p = part + static_cast<int64_t>(blockIdx.x) * PART;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) p[(2 * ti + a) + 32 * (2 * tj + b)] = acc[a][b];
+}
+
+// Upper Cholesky G = R^T R of the k x k matrix in G (stride 33) by warp 0,
+// written as compact code (runtime loops): it runs once per panel on one warp,
+// so what matters is the instruction count per pivot. Lane i carries the
+// residual of row i in a register window d[j] = G[i][kb + j] that shifts left
+// by four columns per block step. A block step factors four pivots (the 4 x 4
+// diagonal block through shuffles), publishes the four new columns of L as one
+// float4 per lane in shared memory, and applies the rank-4 update to the
+// window with one float4 load per column. Pivots are d * rsqrt(d) (the factor
+// only has to be used consistently: CholQR2 applies exactly the R it
+// computed). Writes R column-major, Rc[j * RCS + i] = R[i][j] (zeros outside
+// the k x k upper triangle), and rinv[i] = rsqrt of the i-th pivot, 1 / R[i][i]
+// to within an ulp. Fails (*okout = 0) on a pivot below 1e-4 of its column's
+// original diagonal, a non-finite value, or, with `near_identity`,
+// max |G - I| > 1/4.
+__device__ __forceinline__ void chol_upper(const float* G, int k, float* Rc, float* rinv, bool near_identity,
+                                           int* okout) {
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  float* Lb = Rc;  // scratch for the published block columns reuses Rc's layout: Lb[lane * RCS + kb .. kb+3]
+  float d[32];
+  float dev = 0.f;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const float g = (lane < k && j < k) ? G[lane * 33 + j] : 0.f;
+    d[j] = j <= lane ? g : 0.f;
+    if (lane < k && j < k) dev = fmaxf(dev, fabsf(g - (j == lane ? 1.f : 0.f)));
+  }
+  bool ok = true;
+  if (near_identity) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dev = fmaxf(dev, __shfl_xor_sync(0xffffffffu, dev, o));
+    if (!(dev <= 0.25f)) ok = false;
+  }
+  const float gdiag = lane < k ? G[lane * 33 + lane] : 1.f;
+  for (int kb = 0; kb < k; kb += 4) {
+    // four pivots of the block: lane i's L[i][kb + b] in l[b]
+    float l[4];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int kk = kb + b;
+      float lb = 0.f;
+      if (kk < k) {  // warp-uniform
+        float dk = __shfl_sync(0xffffffffu, d[b], kk);
+        const float gk = __shfl_sync(0xffffffffu, gdiag, kk);
+        if (!(dk > 1e-4f * gk) || !(dk < 3.0e38f)) {
+          ok = false;
+          dk = 1.f;
+        }
+        const float ri = rsqrtf(dk);
+        lb = lane == kk ? dk * ri : ((lane > kk && lane < k) ? d[b] * ri : 0.f);
+        if (lane == kk) rinv[kk] = ri;
+        // update the rest of the block's four columns inside the window
+#pragma unroll
+        for (int c = b + 1; c < 4; ++c) {
+          const float lc = __shfl_sync(0xffffffffu, lb, kb + c < 32 ? kb + c : 0);
+          if (kb + c <= lane) d[c] -= lb * lc;
+        }
+      }
+      l[b] = lb;
+    }
+    *reinterpret_cast<float4*>(&Lb[lane * RCS + kb]) = make_float4(l[0], l[1], l[2], l[3]);
+    __syncwarp();
+    // rank-4 update of the window columns kb + 4 .. and shift by four
+#pragma unroll
+    for (int j = 4; j < 32; ++j) {
+      const int c = kb + j;
+      float nv = d[j];
+      if (c < 32) {
+        const float4 lc = *reinterpret_cast<const float4*>(&Lb[c * RCS + kb]);  // L[c][kb .. kb+3]
+        if (c <= lane) nv = fmaf(-l[3], lc.w, fmaf(-l[2], lc.z, fmaf(-l[1], lc.y, fmaf(-l[0], lc.x, nv))));
+      }
+      d[j - 4] = nv;
+    }
+#pragma unroll
+    for (int j = 28; j < 32; ++j) d[j] = 0.f;
+    __syncwarp();
+  }
+  // Rc already holds L[i][j] at i * RCS + j = R[j][i] for j < k (rounded up to a
+  // multiple of 4, zeros beyond k); clear the rest of the 32 x 32 factor.
+  for (int j = (k + 3) & ~3; j < 32; ++j) Rc[lane * RCS + j] = 0.f;
+  if (lane == 0) *okout = ok ? 1 : 0;
+  __syncwarp();
+}
+
+// x R = a for row r of the k columns X[c * ld + r], c < k, in place (R upper
+// k x k column-major in Rc, rinv its reciprocal pivots). Blocks of 8 columns:
+// the 8 x 8 diagonal block in registers, then the later columns in shared
+// memory, reading R as float4 pairs.
+__device__ __forceinline__ void rows_solve(float* X, int ld, int k, int r, const float* Rc, const float* rinv) {
+  for (int b = 0; b < k; b += 8) {
+    float x[8];
+#pragma unroll
+    for (int l = 0; l < 8; ++l) x[l] = b + l < k ? X[(b + l) * ld + r] : 0.f;
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      if (b + l < k) {
+        x[l] *= rinv[b + l];
+#pragma unroll
+        for (int j = l + 1; j < 8; ++j) x[j] -= x[l] * Rc[(b + j) * RCS + b + l];
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < 8; ++l)
+      if (b + l < k) X[(b + l) * ld + r] = x[l];
+#pragma unroll 4
+    for (int j = b + 8; j < k; ++j) {
+      const float4 r0 = *reinterpret_cast<const float4*>(&Rc[j * RCS + b]);
+      const float4 r1 = *reinterpret_cast<const float4*>(&Rc[j * RCS + b + 4]);
+      float t = X[j * ld + r];
+      t = fmaf(-x[0], r0.x, t);
+      t = fmaf(-x[1], r0.y, t);
+      t = fmaf(-x[2], r0.z, t);
+      t = fmaf(-x[3], r0.w, t);
+      t = fmaf(-x[4], r1.x, t);
+      t = fmaf(-x[5], r1.y, t);
+      t = fmaf(-x[6], r1.z, t);
+      t = fmaf(-x[7], r1.w, t);
+      X[j * ld + r] = t;
+    }
+  }
+}
+
+__device__ __forceinline__ void put_shadow(char* hi, char* lo, int64_t o, float v, int mode) {
+  if (!hi) return;
+  if (mode == 1) {
+    reinterpret_cast<__nv_bfloat16*>(hi)[o] = __float2bfloat16_rn(v);
+  } else {
+    const __half h = __float2half_rn(v);
+    reinterpret_cast<__half*>(hi)[o] = h;
+    if (mode == 2) reinterpret_cast<__half*>(lo)[o] = __float2half_rn((v - __half2float(h)) * 2048.f);
+  }
+}
+
+// MGS-TSQR of the panel (the multi-launch path's algorithm) over virtual blocks.
+__device__ bool panel_tsqr(const LeafPlan& P, TsqrReduceSmem& tr, TsqrApplySmem& ta, GridSync& gs, int* okflag, int c0,
+                           int k) {
+  TsqrPlan T = P.tsqr;
+  T.lev[0] = P.A + static_cast<int64_t>(c0) * P.lda;
+  T.ld[0] = P.lda;
+  T.R = P.R + c0 + static_cast<int64_t>(c0) * P.ldr;
+  T.ldr = P.ldr;
+  T.ncols = k;
+  for (int b = blockIdx.x; b < T.nblk[0]; b += gridDim.x) tsqr_reduce_block(T, b, tr);
+  if (!grid_barrier(gs, okflag)) return false;
+  char* qh = P.qh ? P.qh + static_cast<int64_t>(c0) * P.ldh * 2 : nullptr;
+  char* ql = P.ql ? P.ql + static_cast<int64_t>(c0) * P.ldh * 2 : nullptr;
+  const int nb = (P.m + BR - 1) / BR;
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) tsqr_apply_rows(T, b * BR, qh, ql, P.ldh, P.mode, ta);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && P.fallbacks) atomicAdd(P.fallbacks, 1);
+  return grid_barrier(gs, okflag);
+}
+
+// CholQR2 of columns [c0, c0 + k) over the CTA's slab [r0, r1); false when a
+// barrier gave up.
+__device__ bool panel_step(const LeafPlan& P, LeafSmem& sm, GridSync& gs, int* okflag, int c0, int k, int r0,
+                           int r1) {
+  PanelSmem& ps = sm.p;
+  const float* Ac = P.A + static_cast<int64_t>(c0) * P.lda;
+  const int tid = threadIdx.x;
+  // ---- G = A^T A
+  {
+    float acc[2][2] = {};
+    for (int t0 = r0; t0 < r1; t0 += GT) {
+      const int rows = min(GT, r1 - t0);
+      batched_copy(
+          32 * GT,
+          [&](int e) {
+            const int r = e % GT, c = e / GT;
+            return (r < rows && c < k) ? __ldcg(&Ac[t0 + r + static_cast<int64_t>(c) * P.lda]) : 0.f;
+          },
+          [&](int e, float v) { ps.S[(e / GT) * (GT + 1) + e % GT] = v; });
+      __syncthreads();
+      gram_tile(ps.S, rows, acc);
+      __syncthreads();
+    }
+    write_gram_partial(P.part, acc);
+  }
+  if (!grid_barrier(gs, okflag)) return false;
+  reduce_partials(P.part, 32, 32, 32, [&](int e, float v) { P.red[e] = v; });
+  if (!grid_barrier(gs, okflag)) return false;
+  // ---- R1 = chol(G); Q1 = A R1^-1 (scratch); G2 = Q1^T Q1
+  for (int e = tid; e < 1024; e += LT) ps.G[(e % 32) * 33 + e / 32] = __ldcg(&P.red[e]);
+  __syncthreads();
+  chol_upper(ps.G, k, ps.R1, ps.rinv1, false, &ps.ok);
+  __syncthreads();
+  if (!ps.ok) return panel_tsqr(P, sm.tr, sm.ta, gs, okflag, c0, k);
+  {
+    float acc[2][2] = {};
+    for (int t0 = r0; t0 < r1; t0 += GT) {
+      const int rows = min(GT, r1 - t0);
+      batched_copy(
+          32 * GT,
+          [&](int e) {
+            const int r = e % GT, c = e / GT;
+            return (r < rows && c < k) ? __ldcg(&Ac[t0 + r + static_cast<int64_t>(c) * P.lda]) : 0.f;
+          },
+          [&](int e, float v) { ps.S[(e / GT) * (GT + 1) + e % GT] = v; });
+      __syncthreads();
+      if (tid < rows) rows_solve(ps.S, GT + 1, k, tid, ps.R1, ps.rinv1);
+      __syncthreads();
+      if (tid < rows) {
+        for (int j = 0; j < k; ++j) P.q1[t0 + tid + static_cast<int64_t>(j) * P.m] = ps.S[j * (GT + 1) + tid];
+      }
+      gram_tile(ps.S, rows, acc);
+      __syncthreads();
+    }
+    write_gram_partial(P.part, acc);
+  }
+  if (!grid_barrier(gs, okflag)) return false;
+  reduce_partials(P.part, 32, 32, 32, [&](int e, float v) { P.red[e] = v; });
+  if (!grid_barrier(gs, okflag)) return false;
+  // ---- R2 = chol(G2) (near the identity); Q = Q1 R2^-1; R = R2 R1
+  for (int e = tid; e < 1024; e += LT) ps.G[(e % 32) * 33 + e / 32] = __ldcg(&P.red[e]);
+  __syncthreads();
+  chol_upper(ps.G, k, ps.R2, ps.rinv2, true, &ps.ok);
+  __syncthreads();
+  if (!ps.ok) return panel_tsqr(P, sm.tr, sm.ta, gs, okflag, c0, k);
+  float* Aw = P.A + static_cast<int64_t>(c0) * P.lda;
+  char* qh = P.qh ? P.qh + static_cast<int64_t>(c0) * P.ldh * 2 : nullptr;
+  char* ql = P.ql ? P.ql + static_cast<int64_t>(c0) * P.ldh * 2 : nullptr;
+  for (int t0 = r0; t0 < r1; t0 += GT) {
+    const int rows = min(GT, r1 - t0);
+    batched_copy(
+        32 * GT,
+        [&](int e) {
+          const int r = e % GT, c = e / GT;
+          return (r < rows && c < k) ? __ldcg(&P.q1[t0 + r + static_cast<int64_t>(c) * P.m]) : 0.f;
+        },
+        [&](int e, float v) { ps.S[(e / GT) * (GT + 1) + e % GT] = v; });
+    __syncthreads();
+    if (tid < rows) {
+      rows_solve(ps.S, GT + 1, k, tid, ps.R2, ps.rinv2);
+      const int r = t0 + tid;
+      for (int j = 0; j < k; ++j) {
+        const float v = ps.S[j * (GT + 1) + tid];
+        Aw[r + static_cast<int64_t>(j) * P.lda] = v;
+        put_shadow(qh, ql, r + static_cast<int64_t>(j) * P.ldh, v, P.mode);
+      }
+    }
+    __syncthreads();
+  }
+  if (blockIdx.x == 0) {
+    for (int e = tid; e < 1024; e += LT) {
+      const int i = e % 32, j = e / 32;
+      if (i < k && j < k) {
+        float sum = 0.f;
+        for (int l = i; l <= j; ++l) sum += ps.R2[l * RCS + i] * ps.R1[j * RCS + l];
+        P.R[(c0 + i) + static_cast<int64_t>(c0 + j) * P.ldr] = i <= j ? sum : 0.f;
+      }
+    }
+  }
+  return true;
+}
+
+// A2 -= Q (Q^T A2) for Q = columns [c0, c0 + w1), A2 = [c1, c1 + w2) over the
+// CTA's slab; the product is written (pass 0) or added (pass 1) into R.
+__device__ bool update_step(const LeafPlan& P, LeafSmem& sm, GridSync& gs, int* okflag, const LeafStep& s, int r0,
+                            int r1, int pass) {
+  UpdateSmem& us = sm.u;
+  const float* Q = P.A + static_cast<int64_t>(s.c0) * P.lda;
+  float* A2 = P.A + static_cast<int64_t>(s.c1) * P.lda;
+  const int tid = threadIdx.x;
+  const int ti = tid / 16, tj = tid % 16;
+  {
+    float acc[4][4] = {};
+    for (int t0 = r0; t0 < r1; t0 += UT) {
+      const int rows = min(UT, r1 - t0);
+      batched_copy(
+          UT * 64,
+          [&](int e) {
+            const int r = e % UT, c = e / UT;
+            return (r < rows && c < s.w1) ? __ldcg(&Q[t0 + r + static_cast<int64_t>(c) * P.lda]) : 0.f;
+          },
+          [&](int e, float v) { us.Qs[(e % UT) * SP + e / UT] = v; });
+      batched_copy(
+          UT * 64,
+          [&](int e) {
+            const int r = e % UT, c = e / UT;
+            return (r < rows && c < s.w2) ? __ldcg(&A2[t0 + r + static_cast<int64_t>(c) * P.lda]) : 0.f;
+          },
+          [&](int e, float v) { us.As[(e % UT) * SP + e / UT] = v; });
+      __syncthreads();
+#pragma unroll 4
+      for (int r = 0; r < rows; ++r) {
+        const float4 q = *reinterpret_cast<const float4*>(&us.Qs[r * SP + 4 * ti]);
+        const float4 a = *reinterpret_cast<const float4*>(&us.As[r * SP + 4 * tj]);
+        const float qv[4] = {q.x, q.y, q.z, q.w};
+        const float av[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] += qv[u] * av[v];
+      }
+      __syncthreads();
+    }
+    float* p = P.part + static_cast<int64_t>(blockIdx.x) * PART;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) p[(4 * ti + u) + 64 * (4 * tj + v)] = acc[u][v];
+  }
+  if (!grid_barrier(gs, okflag)) return false;
+  reduce_partials(
+      P.part, s.w1, s.w2, 64,
+      [&](int e, float v) {
+        P.red[e] = v;
+        float* rp = &P.R[(s.c0 + e % 64) + static_cast<int64_t>(s.c1 + e / 64) * P.ldr];
+        *rp = pass ? *rp + v : v;
+      });
+  if (!grid_barrier(gs, okflag)) return false;
+  batched_copy(
+      64 * 64,
+      [&](int e) { return ((e % 64) < s.w1 && (e / 64) < s.w2) ? __ldcg(&P.red[e]) : 0.f; },
+      [&](int e, float v) { us.Ps[(e % 64) * SP + e / 64] = v; });
+  for (int t0 = r0; t0 < r1; t0 += UT) {
+    const int rows = min(UT, r1 - t0);
+    batched_copy(
+        UT * 64,
+        [&](int e) {
+          const int r = e % UT, c = e / UT;
+          return (r < rows && c < s.w1) ? __ldcg(&Q[t0 + r + static_cast<int64_t>(c) * P.lda]) : 0.f;
+        },
+        [&](int e, float v) { us.Qs[(e % UT) * SP + e / UT] = v; });
+    __syncthreads();
+    // thread (ti, tj): rows 4ti.., columns 4tj..
+    float acc[4][4] = {};
+    for (int i = 0; i < s.w1; i += 4) {
+      float4 q[4], pr[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) q[u] = *reinterpret_cast<const float4*>(&us.Qs[(4 * ti + u) * SP + i]);
+#pragma unroll
+      for (int l = 0; l < 4; ++l) pr[l] = *reinterpret_cast<const float4*>(&us.Ps[(i + l) * SP + 4 * tj]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float qv[4] = {q[u].x, q[u].y, q[u].z, q[u].w};
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+          acc[u][0] += qv[l] * pr[l].x;
+          acc[u][1] += qv[l] * pr[l].y;
+          acc[u][2] += qv[l] * pr[l].z;
+          acc[u][3] += qv[l] * pr[l].w;
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int r = 4 * ti + u;
+      if (r < rows) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int j = 4 * tj + v;
+          if (j < s.w2) {
+            float* ap = &A2[t0 + r + static_cast<int64_t>(j) * P.lda];
+            *ap = __ldcg(ap) - acc[u][v];
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// ================================================================ resident leaf
+// When every CTA's slab is at most RMAX rows, the slab (all w columns) stays
+// in shared memory for the whole leaf, column-major with stride XS: one read
+// of the leaf from HBM, one write of Q, and every phase in between works on
+// shared memory (float4 along rows). The panel's first-pass Q1 goes to a
+// separate buffer Y so that the MGS-TSQR fallback still finds the panel as it
+// was.
+constexpr int RMAX = 256;
+constexpr int XS = RMAX + 4;
+
+struct ResPanelSmem {
+  float G[32 * 33];
+  float R1[32 * RCS];  // column-major factors
+  float R2[32 * RCS];
+  float rinv1[32];
+  float rinv2[32];
+  int ok;
+};
+
+struct ResSmem {
+  float X[kLeafMaxWidth * XS];
+  float Y[32 * XS];
+  float gp[4096];  // per-row-group partial products
+  union {
+    ResPanelSmem p;
+    float Ps[64 * SP];  // P = Q^T A2, row-major
+    TsqrReduceSmem tr;
+    TsqrApplySmem ta;
+  };
+};
+
+// Loads rows [r0, r0 + rows) of the leaf's w columns into X; rows [rows, RMAX) are zeroed.
+__device__ void res_load(const LeafPlan& P, float* X, int r0, int rows, int cols) {
+  const int tid = threadIdx.x;
+  const int zr = RMAX - rows;
+  for (int e = tid; e < zr * cols; e += LT) X[(e / zr) * XS + rows + e % zr] = 0.f;
+  if (P.vec) {
+    const int nq = rows / 4, total = nq * cols;
+    for (int base = tid; base < total; base += 8 * LT) {
+      float4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * LT;
+        v[u] = e < total ? __ldcg(reinterpret_cast<const float4*>(P.A + r0 + 4 * (e % nq) +
+                                                                  static_cast<int64_t>(e / nq) * P.lda))
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * LT;
+        if (e < total) *reinterpret_cast<float4*>(&X[(e / nq) * XS + 4 * (e % nq)]) = v[u];
+      }
+    }
+    const int tr = rows - 4 * nq;
+    for (int e = tid; e < tr * cols; e += LT) {
+      const int r = 4 * nq + e % tr, c = e / tr;
+      X[c * XS + r] = __ldcg(&P.A[r0 + r + static_cast<int64_t>(c) * P.lda]);
+    }
+  } else if (rows > 0) {
+    batched_copy(
+        rows * cols, [&](int e) { return __ldcg(&P.A[r0 + e % rows + static_cast<int64_t>(e / rows) * P.lda]); },
+        [&](int e, float v) { X[(e / rows) * XS + e % rows] = v; });
+  }
+}
+
+// Writes columns [c0, c0 + cols) of the slab back to A (and Q's 16-bit copy when `shadow`).
+__device__ void res_store(const LeafPlan& P, const float* X, int r0, int rows, int c0, int cols, bool shadow) {
+  const int tid = threadIdx.x;
+  if (P.vec) {
+    const int nq = rows / 4, total = nq * cols;
+    for (int e = tid; e < total; e += LT) {
+      const int c = c0 + e / nq, q = e % nq;
+      *reinterpret_cast<float4*>(P.A + r0 + 4 * q + static_cast<int64_t>(c) * P.lda) =
+          *reinterpret_cast<const float4*>(&X[c * XS + 4 * q]);
+    }
+    const int tr = rows - 4 * nq;
+    for (int e = tid; e < tr * cols; e += LT) {
+      const int r = 4 * nq + e % tr, c = c0 + e / tr;
+      P.A[r0 + r + static_cast<int64_t>(c) * P.lda] = X[c * XS + r];
+    }
+  } else {
+    for (int e = tid; e < rows * cols; e += LT) {
+      const int r = e % rows, c = c0 + e / rows;
+      P.A[r0 + r + static_cast<int64_t>(c) * P.lda] = X[c * XS + r];
+    }
+  }
+  if (shadow && P.qh) {
+    for (int e = tid; e < rows * cols; e += LT) {
+      const int r = e % rows, c = c0 + e / rows;
+      put_shadow(P.qh, P.ql, r0 + r + static_cast<int64_t>(c) * P.ldh, X[c * XS + r], P.mode);
+    }
+  }
+}
+
+// Partial product Xa^T Xb of the slab (Xa = columns [a0, a0 + na) of `Xa`,
+// Xb = columns [b0, b0 + nb) of `Xb`, na, nb <= 64) into part (entry i + 64 j).
+// Threads form row groups when the output needs fewer than 256 4x4 tiles; the
+// groups' sums are added in group order.
+__device__ void res_tn(const float* Xa, int a0, int na, const float* Xb, int b0, int nb, int rows_eff, float* gp,
+                       float* part) {
+  const int tid = threadIdx.x;
+  const int nta = (na + 3) / 4, ntb = (nb + 3) / 4, nt = nta * ntb;
+  const int groups = max(1, LT / nt);
+  const int g = tid / nt, t = tid % nt;
+  const int ti = t % nta, tj = t / nta;
+  const int npad = 16 * nt;
+  if (g < groups) {
+    const int chunk = ((rows_eff / 4 + groups - 1) / groups) * 4;
+    const int rb = g * chunk, re = min(rows_eff, rb + chunk);
+    float acc[4][4] = {};
+    // thread (ti, tj) owns columns ti + nta u of Xa and tj + ntb v of Xb: with XS = 4 x odd,
+    // the eight float4 rows a warp reads at once fall in eight different bank groups
+    const float* pa = Xa + (a0 + ti) * XS;
+    const float* pb = Xb + (b0 + tj) * XS;
+#pragma unroll 2
+    for (int r = rb; r < re; r += 4) {
+      float4 a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = *reinterpret_cast<const float4*>(&pa[u * nta * XS + r]);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) b[v] = *reinterpret_cast<const float4*>(&pb[v * ntb * XS + r]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          acc[u][v] = fmaf(a[u].w, b[v].w, fmaf(a[u].z, b[v].z, fmaf(a[u].y, b[v].y, fmaf(a[u].x, b[v].x, acc[u][v]))));
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) gp[g * npad + (ti + nta * u) + 4 * nta * (tj + ntb * v)] = acc[u][v];
+  }
+  __syncthreads();
+  float* p = part + static_cast<int64_t>(blockIdx.x) * PART;
+  for (int e = tid; e < npad; e += LT) {
+    float s = 0.f;
+    for (int gg = 0; gg < groups; ++gg) s += gp[gg * npad + e];
+    p[e % (4 * nta) + 64 * (e / (4 * nta))] = s;
+  }
+}
+
+// Panel fallback: the slab's columns [c0, c0 + k) go back to A, MGS-TSQR runs
+// on A (the reference's algorithm), and the factored columns come back.
+__device__ bool res_fallback(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, int c0, int k, int r0,
+                             int rows) {
+  res_store(P, S.X, r0, rows, c0, k, false);
+  if (!grid_barrier(gs, okflag)) return false;
+  if (!panel_tsqr(P, S.tr, S.ta, gs, okflag, c0, k)) return false;
+  for (int e = threadIdx.x; e < rows * k; e += LT) {
+    const int r = e % rows, c = c0 + e / rows;
+    S.X[c * XS + r] = __ldcg(&P.A[r0 + r + static_cast<int64_t>(c) * P.lda]);
+  }
+  __syncthreads();
+  return true;
+}
+
+// D[:, dc + j] = S0[:, sc + j] - sum_{i < K} Sq[:, qc + i] P[i][j] for j < nj
+// over the slab's rows (P row-major with stride ldp in shared memory; D may be
+// S0). 4 rows x 4 columns per tile, float4 along rows.
+__device__ void slab_gemm_sub(float* D, int dc, const float* S0, int sc, const float* Sq, int qc, int K,
+                              const float* Pm, int ldp, int nj, int rows_eff) {
+  const int nrt = rows_eff / 4, nct = (nj + 3) / 4;
+  for (int t = threadIdx.x; t < nrt * nct; t += LT) {
+    const int rt = t % nrt, ct = t / nrt;
+    float acc[4][4] = {};
+#pragma unroll 4
+    for (int i = 0; i < K; ++i) {
+      const float4 q = *reinterpret_cast<const float4*>(&Sq[(qc + i) * XS + 4 * rt]);
+      const float4 pp = *reinterpret_cast<const float4*>(&Pm[i * ldp + 4 * ct]);
+      const float qv[4] = {q.x, q.y, q.z, q.w};
+      const float pv[4] = {pp.x, pp.y, pp.z, pp.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(qv[u], pv[v], acc[u][v]);
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      if (4 * ct + v < nj) {
+        const float4 x = *reinterpret_cast<const float4*>(&S0[(sc + 4 * ct + v) * XS + 4 * rt]);
+        *reinterpret_cast<float4*>(&D[(dc + 4 * ct + v) * XS + 4 * rt]) =
+            make_float4(x.x - acc[0][v], x.y - acc[1][v], x.z - acc[2][v], x.w - acc[3][v]);
+      }
+    }
+  }
+}
+
+// Y R = A for the slab rows (Y = columns 0 .. k-1 of `Y`, in place; R upper
+// k x k column-major in Rc): per block of 8 columns, each thread solves its
+// row's 8 x 8 diagonal block (a chain of 8), then the columns after the block
+// are updated by all threads as a small tiled product (no chain). Rt is a
+// 8 x RCS scratch for the block's rows of R.
+__device__ void slab_solve(float* Y, int k, int rows, int rows_eff, const float* Rc, const float* rinv, float* Rt) {
+  const int tid = threadIdx.x;
+  for (int b = 0; b < k; b += 8) {
+    if (tid < rows) {
+      float x[8];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) x[l] = b + l < k ? Y[(b + l) * XS + tid] : 0.f;
+#pragma unroll
+      for (int l = 0; l < 8; ++l) {
+        if (b + l < k) {
+          x[l] *= rinv[b + l];
+#pragma unroll
+          for (int j = l + 1; j < 8; ++j) x[j] = fmaf(-x[l], Rc[(b + j) * RCS + b + l], x[j]);
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < 8; ++l)
+        if (b + l < k) Y[(b + l) * XS + tid] = x[l];
+    }
+    const int nj = k - b - 8;
+    if (nj > 0) {
+      for (int e = tid; e < 8 * 32; e += LT) {
+        const int i = e / 32, j = e % 32;
+        Rt[i * RCS + j] = (j < nj) ? Rc[(b + 8 + j) * RCS + b + i] : 0.f;
+      }
+    }
+    __syncthreads();
+    if (nj > 0) {
+      slab_gemm_sub(Y, b + 8, Y, b + 8, Y, b, 8, Rt, RCS, nj, rows_eff);
+      __syncthreads();
+    }
+  }
+}
+
+__device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, int c0, int k, int r0,
+                          int rows) {
+  ResPanelSmem& ps = S.p;
+  const int tid = threadIdx.x;
+  const int rows_eff = (rows + 3) & ~3;
+  // ---- G = A^T A
+  res_tn(S.X, c0, k, S.X, c0, k, rows_eff, S.gp, P.part);
+  if (!grid_barrier(gs, okflag)) return false;
+  reduce_partials(P.part, k, k, 64, [&](int e, float v) { P.red[e] = v; });
+  if (!grid_barrier(gs, okflag)) return false;
+  batched_copy(
+      1024, [&](int e) { return ((e % 32) < k && (e / 32) < k) ? __ldcg(&P.red[(e % 32) + 64 * (e / 32)]) : 0.f; },
+      [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
+  __syncthreads();
+  chol_upper(ps.G, k, ps.R1, ps.rinv1, false, &ps.ok);
+  __syncthreads();
+  if (!ps.ok) return res_fallback(P, S, gs, okflag, c0, k, r0, rows);
+  // ---- Y = X R1^-1 (rows of the slab), G2 = Y^T Y
+  for (int e = tid; e < 32 * RMAX; e += LT) {
+    const int c = e / RMAX, r = e % RMAX;
+    S.Y[c * XS + r] = c < k ? S.X[(c0 + c) * XS + r] : 0.f;
+  }
+  __syncthreads();
+  slab_solve(S.Y, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2);
+  res_tn(S.Y, 0, k, S.Y, 0, k, rows_eff, S.gp, P.part);
+  if (!grid_barrier(gs, okflag)) return false;
+  reduce_partials(P.part, k, k, 64, [&](int e, float v) { P.red[e] = v; });
+  if (!grid_barrier(gs, okflag)) return false;
+  batched_copy(
+      1024, [&](int e) { return ((e % 32) < k && (e / 32) < k) ? __ldcg(&P.red[(e % 32) + 64 * (e / 32)]) : 0.f; },
+      [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
+  __syncthreads();
+  // G2 = I + E. When max |E| <= 3e-4, chol(I + E) = I + F + O(E^2) with
+  // F = triu(E) - diag(E) / 2, and Q = Y (I - F) has Q^T Q = I + O(E^2) and
+  // Q (I + F) R1 = Y R1 + O(E^2): no second Cholesky and no second
+  // substitution chain, only a small product. Otherwise the exact path.
+  if (tid < 32) {
+    float dev = 0.f;
+    for (int j = 0; j < k; ++j)
+      if (tid < k) dev = fmaxf(dev, fabsf(ps.G[tid * 33 + j] - (j == tid ? 1.f : 0.f)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dev = fmaxf(dev, __shfl_xor_sync(0xffffffffu, dev, o));
+    if (tid == 0) ps.ok = dev <= 3e-4f ? 2 : 0;
+  }
+  __syncthreads();
+  const bool first_order = ps.ok == 2;
+  if (first_order) {
+    // F row-major (stride RCS) in R2's place
+    for (int e = tid; e < 32 * RCS; e += LT) {
+      const int i = e / RCS, j = e % RCS;
+      float f = 0.f;
+      if (i < k && j < k && i <= j) f = i == j ? 0.5f * (ps.G[i * 33 + i] - 1.f) : ps.G[i * 33 + j];
+      ps.R2[e] = f;
+    }
+    __syncthreads();
+    slab_gemm_sub(S.X, c0, S.Y, 0, S.Y, 0, k, ps.R2, RCS, k, rows_eff);
+  } else {
+    chol_upper(ps.G, k, ps.R2, ps.rinv2, true, &ps.ok);
+    __syncthreads();
+    if (!ps.ok) return res_fallback(P, S, gs, okflag, c0, k, r0, rows);
+    // ---- Q = Y R2^-1 into the slab
+    if (tid < rows) rows_solve(S.Y, XS, k, tid, ps.R2, ps.rinv2);
+    __syncthreads();
+    for (int e = tid; e < k * RMAX; e += LT) {
+      const int c = e / RMAX, r = e % RMAX;
+      if (r < rows) S.X[(c0 + c) * XS + r] = S.Y[c * XS + r];
+    }
+  }
+  // R = R2 R1 (exact) or (I + F) R1 (first order)
+  if (blockIdx.x == 0) {
+    for (int e = tid; e < 1024; e += LT) {
+      const int i = e % 32, j = e / 32;
+      if (i < k && j < k) {
+        float sum = 0.f;
+        if (first_order) {
+          sum = ps.R1[j * RCS + i];
+          for (int l = i; l <= j; ++l) sum = fmaf(ps.R2[i * RCS + l], ps.R1[j * RCS + l], sum);
+        } else {
+          for (int l = i; l <= j; ++l) sum += ps.R2[l * RCS + i] * ps.R1[j * RCS + l];
+        }
+        P.R[(c0 + i) + static_cast<int64_t>(c0 + j) * P.ldr] = i <= j ? sum : 0.f;
+      }
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+__device__ bool res_update(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, const LeafStep& s, int rows,
+                           int pass) {
+  const int rows_eff = (rows + 3) & ~3;
+  res_tn(S.X, s.c0, s.w1, S.X, s.c1, s.w2, rows_eff, S.gp, P.part);
+  if (!grid_barrier(gs, okflag)) return false;
+  reduce_partials(
+      P.part, s.w1, s.w2, 64,
+      [&](int e, float v) {
+        P.red[e] = v;
+        float* rp = &P.R[(s.c0 + e % 64) + static_cast<int64_t>(s.c1 + e / 64) * P.ldr];
+        *rp = pass ? *rp + v : v;
+      });
+  if (!grid_barrier(gs, okflag)) return false;
+  batched_copy(
+      64 * 64, [&](int e) { return ((e % 64) < s.w1 && (e / 64) < s.w2) ? __ldcg(&P.red[e]) : 0.f; },
+      [&](int e, float v) { S.Ps[(e % 64) * SP + e / 64] = v; });
+  __syncthreads();
+  // A2 -= Q P
+  slab_gemm_sub(S.X, s.c1, S.X, s.c1, S.X, s.c0, s.w1, S.Ps, SP, s.w2, rows_eff);
+  __syncthreads();
+  return true;
+}
+
+__global__ void __launch_bounds__(LT, 1) leaf_res_kernel(LeafPlan P) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  ResSmem& S = *reinterpret_cast<ResSmem*>(smraw);
+  __shared__ int okflag;
+  GridSync gs{P.sync, P.sync + 2, P.status, P.budget, 0};
+  const int r0 = min(P.m, static_cast<int>(blockIdx.x) * P.rpc);
+  const int rows = min(P.m, r0 + P.rpc) - r0;
+  res_load(P, S.X, r0, rows, P.w);
+  __syncthreads();
+  bool ok = true;
+  for (int i = 0; i < P.nsteps && ok; ++i) {
+    const LeafStep s = P.step[i];
+    __syncthreads();
+    if (s.kind == 0) {
+      ok = res_panel(P, S, gs, &okflag, s.c0, s.w1, r0, rows);
+    } else {
+      ok = res_update(P, S, gs, &okflag, s, rows, 0);
+      if (ok && P.cgs2) ok = res_update(P, S, gs, &okflag, s, rows, 1);
+    }
+  }
+  __syncthreads();
+  if (ok) res_store(P, S.X, r0, rows, 0, P.w, true);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int prev = atomicAdd(P.sync + 1, 1);
+    if (prev == static_cast<int>(gridDim.x) - 1) {
+      atomicExch(P.sync, 0);
+      atomicExch(P.sync + 2, 0);
+      atomicExch(P.sync + 1, 0);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(LT, 1) leaf_kernel(LeafPlan P) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  LeafSmem& sm = *reinterpret_cast<LeafSmem*>(smraw);
+  __shared__ int okflag;
+  GridSync gs{P.sync, P.sync + 2, P.status, P.budget, 0};
+  const int r0 = min(P.m, static_cast<int>(blockIdx.x) * P.rpc);
+  const int r1 = min(P.m, r0 + P.rpc);
+  for (int i = 0; i < P.nsteps; ++i) {
+    const LeafStep s = P.step[i];
+    bool ok = true;
+    __syncthreads();  // the phases share one shared-memory union: the previous step's readers are done
+    if (s.kind == 0) {
+      ok = panel_step(P, sm, gs, &okflag, s.c0, s.w1, r0, r1);
+    } else {
+      ok = update_step(P, sm, gs, &okflag, s, r0, r1, 0);
+      __syncthreads();
+      if (ok && P.cgs2) ok = update_step(P, sm, gs, &okflag, s, r0, r1, 1);
+    }
+    if (!ok) break;
+  }
+  // Exit protocol: the last CTA out resets the counters for the next launch.
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int prev = atomicAdd(P.sync + 1, 1);
+    if (prev == static_cast<int>(gridDim.x) - 1) {
+      atomicExch(P.sync, 0);
+      atomicExch(P.sync + 2, 0);
+      atomicExch(P.sync + 1, 0);
+    }
+  }
+}
+
+void build_steps(int w, int c0, LeafPlan* P) {
+  if (w <= 32) {
+    P->step[P->nsteps++] = LeafStep{0, c0, w, 0, 0};
+    return;
+  }
+  const int w1 = ((w / 32 + 1) / 2) * 32, w2 = w - w1;  // split_half
+  build_steps(w1, c0, P);
+  P->step[P->nsteps++] = LeafStep{1, c0, w1, c0 + w1, w2};
+  build_steps(w2, c0 + w1, P);
+}
+
+// Resident-kernel grid for m rows, or 0 when a slab would exceed RMAX rows or
+// the device cannot hold one CTA per SM with the resident shared memory.
+int leaf_res_grid(int m, int* rpc) {
+  static int cached[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int g = std::min(num_sms(), (m + RMAX - 1) / RMAX);
+  *rpc = static_cast<int>(round_up((m + g - 1) / g, 4));
+  if (*rpc > RMAX) return 0;
+  int per_sm = dev < 64 ? cached[dev] : 0;
+  if (per_sm == 0) {
+    if (cudaFuncSetAttribute(leaf_res_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(sizeof(ResSmem))) != cudaSuccess)
+      return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, leaf_res_kernel, LT, sizeof(ResSmem)) != cudaSuccess)
+      return 0;
+    if (per_sm < 1) per_sm = -1;
+    if (dev < 64) cached[dev] = per_sm;
+  }
+  return per_sm > 0 ? g : 0;
+}
+
+int leaf_grid(int m) {
+  static int cached[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int per_sm = 0;
+  if (dev < 64 && cached[dev]) {
+    per_sm = cached[dev];
+  } else {
+    if (cudaFuncSetAttribute(leaf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(sizeof(LeafSmem))) != cudaSuccess)
+      return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, leaf_kernel, LT, sizeof(LeafSmem)) != cudaSuccess)
+      return 0;
+    if (dev < 64) cached[dev] = per_sm;
+  }
+  if (per_sm < 1) return 0;
+  const int g = std::min(num_sms(), (m + 63) / 64);
+  return std::max(1, g);
+}
+
+}  // namespace
+
+int64_t leaf_fused_work(int m) {
+  TsqrPlan plan{};
+  int ncnt = 0;
+  int64_t stack = 0;
+  tsqr_plan_sizes(m, &plan, &stack, &ncnt);
+  return static_cast<int64_t>(m) * 32 + static_cast<int64_t>(num_sms()) * PART + PART + stack +
+         64 * (kMaxTsqrLevels + 4);
+}
+
+later_status_t leaf_fused(cudaStream_t st, int m, int w, float* A, int64_t lda, float* R, int64_t ldr, void* qh,
+                          void* ql, int64_t ldh, int out_prec, int cgs2, Arena& ws, int* sync, int* tsqr_counters,
+                          long long budget, int* fallbacks) {
+  if (w < 1 || w > kLeafMaxWidth || m < w) return LATER_ERR_INVALID_ARG;
+  int res_rpc = 0;
+  const int res_grid = leaf_res_grid(m, &res_rpc);
+  const bool resident = res_grid > 0;
+  const int grid = resident ? res_grid : leaf_grid(m);
+  if (grid < 1) return LATER_ERR_NOT_SUPPORTED;
+  LeafPlan P{};
+  P.m = m;
+  P.w = w;
+  P.rpc = resident ? res_rpc : (m + grid - 1) / grid;
+  P.vec = (reinterpret_cast<uintptr_t>(A) % 16 == 0) && (lda % 4 == 0);
+  P.cgs2 = cgs2;
+  P.mode = out_prec == LATER_PREC_BF16 ? 1 : (out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
+  build_steps(w, 0, &P);
+  P.A = A;
+  P.lda = lda;
+  P.R = R;
+  P.ldr = ldr;
+  P.qh = static_cast<char*>(qh);
+  P.ql = static_cast<char*>(ql);
+  P.ldh = ldh;
+  P.sync = sync;
+  P.status = device_status_ptr();
+  P.budget = budget > 0 ? budget : kDefaultBudgetCycles;
+  P.fallbacks = fallbacks;
+  // fallback tree over an m-row panel
+  int64_t stack = 0;
+  int ncnt = 0;
+  tsqr_plan_sizes(m, &P.tsqr, &stack, &ncnt);
+  if (P.tsqr.nblk[P.tsqr.nlev - 1] != 1 || ncnt > 2048) return LATER_ERR_NOT_SUPPORTED;
+  const size_t mark = ws.used();
+  P.q1 = ws.take<float>(static_cast<size_t>(m) * 32);
+  P.part = ws.take<float>(static_cast<size_t>(grid) * PART);
+  P.red = ws.take<float>(PART);
+  for (int L = 1; L < P.tsqr.nlev; ++L) {
+    P.tsqr.ld[L] = round_up(P.tsqr.rows[L], 64);
+    P.tsqr.lev[L] = ws.take<float>(P.tsqr.ld[L] * 32);
+  }
+  if (ws.failed() || !P.q1 || !P.part || !P.red) {
+    ws.reset(mark);
+    return LATER_ERR_WORKSPACE;
+  }
+  P.tsqr.counters = tsqr_counters;
+  P.tsqr.status = P.status;
+  P.tsqr.budget = P.budget;
+  if (ws.sizing()) {
+    ws.reset(mark);
+    return LATER_OK;
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(LT);
+  cfg.dynamicSmemBytes = resident ? sizeof(ResSmem) : sizeof(LeafSmem);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  TraceScope trace(st, TRACE_PANEL);
+  const cudaError_t e = resident ? cudaLaunchKernelEx(&cfg, leaf_res_kernel, P) : cudaLaunchKernelEx(&cfg, leaf_kernel, P);
+  note_launch();
+  ws.reset(mark);
+  return cuda_status(e);
+}
+
+}  // namespace later

@@ -16,6 +16,7 @@
 #include <algorithm>
 
 #include "householder.cuh"
+#include "leaf.cuh"
 #include "panel.cuh"
 #include "qr.cuh"
 
@@ -27,13 +28,14 @@ Options options_from(const later_options_t* o) {
   r.prec = o->precision;
   r.cgs2 = o->cgs2 ? 1 : 0;
   r.leaf = o->leaf > 0 ? o->leaf : 128;
+  r.panel = o->panel;
   r.budget = o->timeout_cycles > 0 ? o->timeout_cycles : kDefaultBudgetCycles;
   return r;
 }
 
 namespace {
 
-constexpr int kCounters = 4096;  // ints: [0,2048) panels, [2048,4096) GEMM split-K
+constexpr int kCounters = 4096 + 64;  // ints: [0,2048) panels, [2048,4096) GEMM split-K, then the fused leaf's sync
 
 struct Ctx {
   cudaStream_t st;
@@ -87,8 +89,20 @@ later_status_t leaf_qr(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t l
   return leaf_qr(c, w2, A2, lda, R + w1 + w1 * ldr, ldr, col + w1);
 }
 
+// A leaf: one fused launch (leaf.cu) unless the caller asked for the
+// reference's panel algorithm or the device / workspace cannot run it.
+later_status_t leaf_top(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
+  if (c.o.panel == 0 && w <= kLeafMaxWidth) {
+    const later_status_t s =
+        leaf_fused(c.st, c.m, w, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
+                   c.o.prec, c.o.cgs2, *c.ws, c.counters + 4096, c.counters, c.o.budget, nullptr);
+    if (s != LATER_ERR_NOT_SUPPORTED && s != LATER_ERR_WORKSPACE) return s;
+  }
+  return leaf_qr(c, w, A, lda, R, ldr, col);
+}
+
 later_status_t rec_qr(Ctx& c, int n, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
-  if (n <= c.o.leaf) return leaf_qr(c, n, A, lda, R, ldr, col);
+  if (n <= c.o.leaf) return leaf_top(c, n, A, lda, R, ldr, col);
   const int n1 = split_half(n), n2 = n - n1;
   LATER_CHECK(rec_qr(c, n1, A, lda, R, ldr, col));
   float* A2 = A + n1 * lda;
@@ -193,7 +207,7 @@ QrNeed rgsqrf_need(int m, int n, const Options& o) {
   const int64_t leaf_parts = ((m + 127) / 128) * 4096 + 128;
   const int64_t splitk = static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 128;
   q.min_work = fixed + std::max<int64_t>(stack, 4096 + 128);
-  q.rec_work = fixed + std::max(std::max(stack, leaf_parts), splitk);
+  q.rec_work = fixed + std::max(std::max(std::max(stack, leaf_parts), splitk), leaf_fused_work(m));
   const int64_t ldh = round_up(m, 8);
   q.hwork = ldh * n * (o.prec == LATER_PREC_SPLIT3 ? 2 : 1);
   return q;

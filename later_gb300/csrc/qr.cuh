@@ -10,6 +10,7 @@ struct Options {
   int prec = LATER_PREC_FP16;
   int cgs2 = 0;
   int leaf = 128;
+  int panel = 0;  // 0: fused CholQR2 leaf (MGS-TSQR fallback); 1: MGS-TSQR panels, separate launches
   long long budget = kDefaultBudgetCycles;
 };
 

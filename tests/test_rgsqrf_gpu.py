@@ -89,3 +89,44 @@ def test_rgsqrf_any_width(cuda, m, n):
     assert metrics.qr_backward_error(A, Q, R) <= max(3 * metrics.qr_backward_error(A, Qo, Ro), 1e-6)
     assert metrics.orthogonality(Q) <= max(3 * metrics.orthogonality(Qo), 1e-5)
     assert np.all(np.tril(R, -1) == 0) and np.all(np.diag(R) > 0)
+
+
+@pytest.mark.parametrize("m,n,prec,cgs2", [(4096, 512, "fp16", False), (2048, 256, "split3", False),
+                                           (16384, 128, "fp16", False), (3001, 200, "bf16", True)])
+def test_fused_leaf_matches_mgs_panels(cuda, m, n, prec, cgs2):
+    """The fused leaf (CholQR2 panels, one launch per leaf) and the reference's panel algorithm
+    (MGS-TSQR, separate launches) give the same factorisation to working accuracy."""
+    A = gen.normal(m, n, seed=7 + m)
+    Qf, Rf = run_gpu(A, precision=prec, cgs2=cgs2)
+    Qm, Rm = run_gpu(A, precision=prec, cgs2=cgs2, panel="mgs")
+    for Q, R in ((Qf, Rf), (Qm, Rm)):
+        assert metrics.qr_backward_error(A, Q, R) <= BOUND_BWD[prec]
+        assert np.all(np.tril(R, -1) == 0) and np.all(np.diag(R) > 0)
+    assert np.linalg.norm(Rf - Rm) / np.linalg.norm(Rm) <= 2 * BOUND_BWD[prec]
+    assert metrics.orthogonality(Qf) <= 2 * metrics.orthogonality(Qm) + 1e-5
+
+
+def test_fused_leaf_falls_back_on_dependent_columns(cuda):
+    """Exactly dependent columns inside a 32-column panel break CholQR2 (a non-positive pivot, or a
+    second Gram matrix far from I); that panel is factored by MGS-TSQR inside the same launch."""
+    A = gen.normal(2048, 128, seed=11)
+    A[:, 5] = A[:, 3]
+    A[:, 70] = 2.0 * A[:, 69]
+    Qf, Rf = run_gpu(A)
+    Qm, Rm = run_gpu(A, panel="mgs")
+    assert np.all(np.isfinite(Qf)) and np.all(np.isfinite(Rf))
+    assert metrics.qr_backward_error(A, Qf, Rf) <= BOUND_BWD["fp16"]
+    scale = np.linalg.norm(A, 2)
+    assert abs(Rf[5, 5]) < 1e-2 * scale and abs(Rf[70, 70]) < 1e-2 * scale
+    # MGS turns a dependent column into normalised rounding noise (so does the reference); the
+    # orthogonality of the other columns is as good as with MGS-TSQR panels throughout.
+    keep = [j for j in range(128) if j not in (5, 70)]
+
+    def orth(Q):
+        Qk = Q[:, keep].astype(np.float64)
+        return np.linalg.norm(Qk.T @ Qk - np.eye(len(keep)))
+
+    assert orth(Qf) <= 4 * orth(Qm) + 0.1, (orth(Qf), orth(Qm))
+    # Panel 0 was factored by the fallback: the same MGS-TSQR arithmetic as the reference's path,
+    # bit for bit (CholQR2 would round differently).
+    assert np.array_equal(Qf[:, :32], Qm[:, :32]) and np.array_equal(Rf[:32, :32], Rm[:32, :32])
