@@ -175,14 +175,16 @@ __device__ void reduce_partials(const float* part, int ni, int nj, int ld, Emit 
     const int q = base + lane;
     const bool has = q < e1;
     const int e = has ? (q % ni) + ld * (q / ni) : 0;
-    float v[8];
+    float sum = 0.f;
+    for (int c0 = warp; c0 < G; c0 += 64) {  // batches of eight CTAs' partials in flight
+      float v[8];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      const int c = warp + 8 * t;
-      v[t] = (has && c < G) ? __ldcg(&part[static_cast<int64_t>(c) * PART + e]) : 0.f;
+      for (int t = 0; t < 8; ++t) {
+        const int c = c0 + 8 * t;
+        v[t] = (has && c < G) ? __ldcg(&part[static_cast<int64_t>(c) * PART + e]) : 0.f;
+      }
+      sum += ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
     }
-    float sum = ((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7]));
-    for (int c = warp + 64; c < G; c += 8) sum += has ? __ldcg(&part[static_cast<int64_t>(c) * PART + e]) : 0.f;
     ws[warp][lane] = sum;
     __syncthreads();
     if (warp == 0 && has) {
@@ -615,10 +617,11 @@ struct ResSmem {
   };
 };
 
-// Loads rows [r0, r0 + rows) of the leaf's w columns into X; rows [rows, RMAX) are zeroed.
+// Loads rows [r0, r0 + rows) of the leaf's w columns into X; rows [rows, rows rounded up to 4)
+// are zeroed (the phases read whole row quads).
 __device__ void res_load(const LeafPlan& P, float* X, int r0, int rows, int cols) {
   const int tid = threadIdx.x;
-  const int zr = RMAX - rows;
+  const int zr = ((rows + 3) & ~3) - rows;
   for (int e = tid; e < zr * cols; e += LT) X[(e / zr) * XS + rows + e % zr] = 0.f;
   if (P.vec) {
     const int nq = rows / 4, total = nq * cols;
@@ -828,8 +831,8 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
   __syncthreads();
   if (!ps.ok) return res_fallback(P, S, gs, okflag, c0, k, r0, rows);
   // ---- Y = X R1^-1 (rows of the slab), G2 = Y^T Y
-  for (int e = tid; e < 32 * RMAX; e += LT) {
-    const int c = e / RMAX, r = e % RMAX;
+  for (int e = tid; e < 32 * rows_eff; e += LT) {
+    const int c = e / rows_eff, r = e % rows_eff;
     S.Y[c * XS + r] = c < k ? S.X[(c0 + c) * XS + r] : 0.f;
   }
   __syncthreads();
@@ -873,8 +876,8 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
     // ---- Q = Y R2^-1 into the slab
     if (tid < rows) rows_solve(S.Y, XS, k, tid, ps.R2, ps.rinv2);
     __syncthreads();
-    for (int e = tid; e < k * RMAX; e += LT) {
-      const int c = e / RMAX, r = e % RMAX;
+    for (int e = tid; e < k * rows_eff; e += LT) {
+      const int c = e / rows_eff, r = e % rows_eff;
       if (r < rows) S.X[(c0 + c) * XS + r] = S.Y[c * XS + r];
     }
   }
@@ -1005,9 +1008,11 @@ int leaf_res_grid(int m, int* rpc) {
   static int cached[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  const int g = std::min(num_sms(), (m + RMAX - 1) / RMAX);
-  *rpc = static_cast<int>(round_up((m + g - 1) / g, 4));
+  // spread the rows over every SM (the phases' time scales with the slab height,
+  // the grid barriers do not), in slabs of a multiple of 4 rows, at most RMAX
+  *rpc = static_cast<int>(round_up((m + num_sms() - 1) / num_sms(), 4));
   if (*rpc > RMAX) return 0;
+  const int g = (m + *rpc - 1) / *rpc;
   int per_sm = dev < 64 ? cached[dev] : 0;
   if (per_sm == 0) {
     if (cudaFuncSetAttribute(leaf_res_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
