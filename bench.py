@@ -51,6 +51,9 @@ def parse():
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--precision", default="fp16", choices=["fp16", "bf16", "split3"])
     p.add_argument("--leaf", type=int, default=128)
+    p.add_argument("--panel", default="fused", choices=["fused", "wide", "mgs"],
+                   help="rgsqrf leaf: fused 32-column CholQR2 panels (default), fused leaf-wide CholQR2 first, "
+                        "or the reference's MGS-TSQR panels")
     p.add_argument("--cgs2", action="store_true")
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--e2e-steps", type=int, default=3)
@@ -179,7 +182,7 @@ def run_reference(a, rank, world):
 def workload_config(a):
     return {"workload": f"rgsqrf {a.m}x{a.n} fp32, N(0,1) seed {a.seed}, {a.precision} tensor-core trailing "
                         f"updates, leaf {a.leaf}{', CGS2' if a.cgs2 else ''}",
-            "m": a.m, "n": a.n, "precision": a.precision, "leaf": a.leaf, "cgs2": a.cgs2,
+            "m": a.m, "n": a.n, "precision": a.precision, "leaf": a.leaf, "cgs2": a.cgs2, "panel": a.panel,
             "l2": "inputs larger than L2 (matrix >= 1 GiB at the default size)"}
 
 
@@ -203,7 +206,7 @@ def run_ours(a, rank, world, local_rank):
     st = torch.cuda.current_stream()
 
     def qr():
-        lg.later_rgsqrf(A, R, work, hwork, precision=a.precision, cgs2=a.cgs2, leaf=a.leaf)
+        lg.later_rgsqrf(A, R, work, hwork, precision=a.precision, cgs2=a.cgs2, leaf=a.leaf, panel=a.panel)
 
     for _ in range(a.warmup):
         A.copy_(A0)

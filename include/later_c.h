@@ -46,8 +46,10 @@ typedef struct {
   int precision;            /* later_precision_t for every tensor-core GEMM */
   int cgs2;                 /* 1: second Gram-Schmidt pass in every panel (CGS2) */
   int leaf;                 /* rgsqrf leaf width: 32, 64 or 128 (0 = 128, the reference's NMIN) */
-  int panel;                /* rgsqrf leaf: 0 = one fused launch per leaf, CholQR2 panels with an
-                               MGS-TSQR fallback (default); 1 = MGS-TSQR panels and separate
+  int panel;                /* rgsqrf leaf: 0 = one fused launch per leaf, CholQR2 per 32-column
+                               panel with an MGS-TSQR fallback (default); 2 = the fused launch
+                               first trying one CholQR2 over the whole leaf (better orthogonality,
+                               slower today), else as 0; 1 = MGS-TSQR panels and separate
                                block-CGS launches (the reference's algorithm) */
   long long timeout_cycles; /* bound on every device wait in SM cycles (0 = about one second) */
 } later_options_t;

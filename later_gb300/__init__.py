@@ -44,7 +44,7 @@ class Options(ctypes.Structure):
     @classmethod
     def make(cls, precision="fp16", cgs2=False, leaf=128, timeout_cycles=0, panel=0) -> "Options":
         p = PREC[precision] if isinstance(precision, str) else int(precision)
-        pn = {"fused": 0, "mgs": 1}[panel] if isinstance(panel, str) else int(panel)
+        pn = {"fused": 0, "mgs": 1, "wide": 2}[panel] if isinstance(panel, str) else int(panel)
         return cls(p, int(bool(cgs2)), int(leaf), pn, int(timeout_cycles))
 
 

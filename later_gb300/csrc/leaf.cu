@@ -40,7 +40,7 @@ constexpr int LT = 256;     // threads per CTA
 constexpr int GT = 256;     // rows per Gram / substitution tile (one per thread)
 constexpr int UT = 64;      // rows per update tile
 constexpr int SP = 68;      // row stride of the update tiles (16-byte rows)
-constexpr int PART = 4096;  // floats per CTA partial (64 x 64)
+constexpr int PART = 8448;  // floats per CTA partial: 64 x 64 (i + 64 j), or a packed 128 x 128 lower triangle
 constexpr int kMaxSteps = 8;
 constexpr int RCS = 36;  // stride of the column-major R factors in shared memory (16-byte columns)
 
@@ -50,7 +50,7 @@ struct LeafStep {
 };
 
 struct LeafPlan {
-  int m, w, rpc, nsteps, cgs2, mode, vec;
+  int m, w, rpc, nsteps, cgs2, mode, vec, wide;
   LeafStep step[kMaxSteps];
   float* A;
   int64_t lda;
@@ -605,15 +605,29 @@ struct ResPanelSmem {
   int ok;
 };
 
+constexpr int MS = 132;   // row stride of the leaf-wide Gram / Cholesky factor (16-byte rows)
+constexpr int RTS = 132;  // row stride of the 8-row slices of R used by the blocked solves
+
 struct ResSmem {
   float X[kLeafMaxWidth * XS];
-  float Y[32 * XS];
-  float gp[4096];  // per-row-group partial products
   union {
-    ResPanelSmem p;
-    float Ps[64 * SP];  // P = Q^T A2, row-major
-    TsqrReduceSmem tr;
-    TsqrApplySmem ta;
+    struct {  // 32-column panels
+      float Y[32 * XS];
+      float gp[4096];  // per-row-group partial products
+      union {
+        ResPanelSmem p;
+        float Ps[64 * SP];  // P = Q^T A2, row-major
+        TsqrReduceSmem tr;
+        TsqrApplySmem ta;
+      };
+    };
+    struct {  // the whole leaf at once
+      float M[kLeafMaxWidth * MS];  // Gram matrix, then L = R^T (lower, row-major) in place; then F
+      float Rt[8 * RTS];            // rows b .. b+7 of R (or of F) for the blocked products
+      float wrinv[kLeafMaxWidth];
+      float gd[kLeafMaxWidth];      // the Gram matrix's diagonal before the factorisation
+      int wok;
+    };
   };
 };
 
@@ -924,6 +938,271 @@ __device__ bool res_update(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okf
   return true;
 }
 
+// ------------------------------------------------------------- leaf-wide CholQR2
+// In place lower Cholesky M = L L^T of the n x n matrix in M (row-major, stride
+// ms, multiple of 4; n <= 128), all 256 threads: right-looking in blocks of 4
+// columns. Thread 0 factors the 4 x 4 diagonal block (pivots d * rsqrt(d), the
+// reciprocal pivots into rinv), one thread per row solves the block column
+// below it, and the CTA applies the rank-4 update to the trailing lower
+// triangle, 8 rows x 1 column per work item with float4 reads of the L rows.
+// *okout = 0 on a pivot below ratio * gd[k] (gd: the diagonal before the
+// factorisation) or a non-finite value.
+__device__ void chol_cta(float* M, int ms, int n, const float* gd, float ratio, float* rinv, int* okout) {
+  const int tid = threadIdx.x;
+  if (tid == 0) *okout = 1;
+  for (int kb = 0; kb < n; kb += 4) {
+    const int kw = min(4, n - kb);
+    __syncthreads();
+    if (tid == 0) {
+      int ok = *okout;
+      for (int a = 0; a < kw; ++a) {
+        float* ra = M + (kb + a) * ms + kb;
+        float d = ra[a];
+        for (int b = 0; b < a; ++b) d = fmaf(-ra[b], ra[b], d);
+        if (!(d > ratio * gd[kb + a]) || !(d < 3.0e38f)) {
+          ok = 0;
+          d = 1.f;
+        }
+        const float ri = rsqrtf(d);
+        ra[a] = d * ri;
+        rinv[kb + a] = ri;
+        for (int c = a + 1; c < kw; ++c) {
+          float* rc = M + (kb + c) * ms + kb;
+          float v = rc[a];
+          for (int b = 0; b < a; ++b) v = fmaf(-rc[b], ra[b], v);
+          rc[a] = v * ri;
+        }
+      }
+      *okout = ok;
+    }
+    __syncthreads();
+    const int t0 = kb + kw, nt = n - t0;
+    if (tid < nt) {  // block column below the diagonal block
+      float* ri_ = M + (t0 + tid) * ms + kb;
+      for (int a = 0; a < kw; ++a) {
+        const float* ra = M + (kb + a) * ms + kb;
+        float v = ri_[a];
+        for (int b = 0; b < a; ++b) v = fmaf(-ri_[b], ra[b], v);
+        ri_[a] = v * rinv[kb + a];
+      }
+    }
+    __syncthreads();
+    if (nt > 0) {  // trailing lower triangle: M[i][j] -= L[i][kb..] . L[j][kb..], t0 <= j <= i < n
+      // thread = (column j, row parity): no index arithmetic beyond a shift, rows i >= j
+      const int j = tid >> 1, par = tid & 1;
+      if (j < nt) {
+        const float4 lj = *reinterpret_cast<const float4*>(&M[(t0 + j) * ms + kb]);
+#pragma unroll 4
+        for (int i = j + par; i < nt; i += 2) {
+          const float4 li = *reinterpret_cast<const float4*>(&M[(t0 + i) * ms + kb]);
+          float* mij = &M[(t0 + i) * ms + t0 + j];
+          *mij = fmaf(-li.w, lj.w, fmaf(-li.z, lj.z, fmaf(-li.y, lj.y, fmaf(-li.x, lj.x, *mij))));
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Packed lower-triangle partial G = X^T X of the slab's first w columns (entry
+// i (i + 1) / 2 + j for j <= i) into part. 4 x 4 tiles over the tile grid's
+// upper half (tile (ti, tj), ti <= tj, columns ti + nt u and tj + nt v: each
+// unordered pair once), float4 along rows.
+__device__ void wide_gram(const float* X, int w, int rows_eff, float* part) {
+  const int nt = (w + 3) / 4;
+  const int ntiles = nt * (nt + 1) / 2;
+  float* p = part + static_cast<int64_t>(blockIdx.x) * PART;
+  for (int t = threadIdx.x; t < ntiles; t += LT) {
+    int ti = static_cast<int>((sqrtf(8.f * t + 1.f) - 1.f) * 0.5f);
+    while (ti * (ti + 1) / 2 > t) --ti;
+    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+    const int tj = t - ti * (ti + 1) / 2;  // tj <= ti
+    const float* pa = X + tj * XS;
+    const float* pb = X + ti * XS;
+    float acc[4][4] = {};
+#pragma unroll 2
+    for (int r = 0; r < rows_eff; r += 4) {
+      float4 a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = *reinterpret_cast<const float4*>(&pa[u * nt * XS + r]);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) b[v] = *reinterpret_cast<const float4*>(&pb[v * nt * XS + r]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          acc[u][v] = fmaf(a[u].w, b[v].w, fmaf(a[u].z, b[v].z, fmaf(a[u].y, b[v].y, fmaf(a[u].x, b[v].x, acc[u][v]))));
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int cj = tj + nt * u, ci = ti + nt * v;  // columns of a and b
+        const int i = max(ci, cj), j = min(ci, cj);
+        if (i < w && (ti != tj || ci >= cj)) p[i * (i + 1) / 2 + j] = acc[u][v];
+      }
+  }
+}
+
+// Loads the reduced packed Gram matrix: diagonal into gd; off-diagonal entries
+// into M's lower triangle (M[i][j], i > j) or, with `upper`, into its upper
+// triangle (M[j][i]) so that a factor already held in the lower triangle stays.
+__device__ void wide_load_gram(const float* red, int w, float* M, float* gd, bool upper) {
+  const int E = w * (w + 1) / 2;
+  batched_copy(
+      E, [&](int e) { return __ldcg(&red[e]); },
+      [&](int e, float v) {
+        int i = static_cast<int>((sqrtf(8.f * e + 1.f) - 1.f) * 0.5f);
+        while (i * (i + 1) / 2 > e) --i;
+        while ((i + 1) * (i + 2) / 2 <= e) ++i;
+        const int j = e - i * (i + 1) / 2;
+        if (i == j) {
+          gd[i] = v;
+          if (!upper) M[i * MS + i] = v;
+        } else {
+          M[upper ? j * MS + i : i * MS + j] = v;
+        }
+      });
+}
+
+// X R = A in place for the slab's first w columns (R upper, R[i][j] = L[j][i] =
+// M[j * MS + i]; rinv its reciprocal pivots): blocks of 8 columns, the 8 x 8
+// diagonal block per row (a chain of 8), the later columns as a tiled product.
+__device__ void wide_solve(float* X, int w, int rows, int rows_eff, const float* M, const float* rinv, float* Rt) {
+  const int tid = threadIdx.x;
+  for (int b = 0; b < w; b += 8) {
+    if (tid < rows) {
+      float x[8];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) x[l] = b + l < w ? X[(b + l) * XS + tid] : 0.f;
+#pragma unroll
+      for (int l = 0; l < 8; ++l) {
+        if (b + l < w) {
+          x[l] *= rinv[b + l];
+#pragma unroll
+          for (int j = l + 1; j < 8; ++j)
+            if (b + j < w) x[j] = fmaf(-x[l], M[(b + j) * MS + b + l], x[j]);
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < 8; ++l)
+        if (b + l < w) X[(b + l) * XS + tid] = x[l];
+    }
+    const int nj = w - b - 8;
+    if (nj > 0) {
+      for (int e = tid; e < 8 * nj; e += LT) {
+        const int i = e / nj, j = e % nj;
+        Rt[i * RTS + j] = M[(b + 8 + j) * MS + b + i];  // R[b + i][b + 8 + j]
+      }
+    }
+    __syncthreads();
+    if (nj > 0) {
+      slab_gemm_sub(X, b + 8, X, b + 8, X, b, 8, Rt, RTS, nj, rows_eff);
+      __syncthreads();
+    }
+  }
+}
+
+// X <- X (I - F) in place, F upper: F[i][j] = M[i * MS + j] for i < j, F[i][i] =
+// fd[i]. Column blocks of 8 from the last to the first, so the columns a block
+// reads are still the old ones: each row takes its block's own 8 x 8 triangle
+// in registers, the columns before the block are applied as one tiled product
+// (F's block column staged row-major, stride 8, in Ft), then the triangle.
+__device__ void wide_apply_f(float* X, int w, int rows, int rows_eff, const float* M, const float* fd, float* Ft) {
+  const int tid = threadIdx.x;
+  for (int b = ((w - 1) / 8) * 8; b >= 0; b -= 8) {
+    const int nb = min(8, w - b);
+    float dpart[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) dpart[j] = 0.f;
+    if (tid < rows) {
+      float x[8];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) x[l] = l < nb ? X[(b + l) * XS + tid] : 0.f;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+#pragma unroll
+        for (int l = 0; l <= j; ++l)
+          if (j < nb) dpart[j] = fmaf(x[l], l == j ? fd[b + j] : M[(b + l) * MS + b + j], dpart[j]);
+    }
+    for (int e = tid; e < b * 8; e += LT) {
+      const int i = e / 8, j = e % 8;
+      Ft[i * 8 + j] = j < nb ? M[i * MS + b + j] : 0.f;
+    }
+    __syncthreads();
+    if (b > 0) {
+      slab_gemm_sub(X, b, X, b, X, 0, b, Ft, 8, nb, rows_eff);
+      __syncthreads();
+    }
+    if (tid < rows) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (j < nb) X[(b + j) * XS + tid] -= dpart[j];
+    }
+    __syncthreads();
+  }
+}
+
+// The whole leaf by CholQR2 at once. Returns 1 when done (Q in the slab, R in
+// P.R), 0 when the leaf is not conditioned well enough for it (nothing has been
+// written; the caller reloads the slab and factors the leaf by 32-column
+// panels), -1 when a grid barrier gave up.
+__device__ int res_wide(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, int rows) {
+  const int tid = threadIdx.x;
+  const int w = P.w;
+  const int rows_eff = (rows + 3) & ~3;
+  const int E = w * (w + 1) / 2;
+  auto put = [&](int e, float v) { P.red[e] = v; };
+  // ---- pass 1: G = X^T X, L = chol(G) (lower triangle of M), X <- X R1^-1
+  wide_gram(S.X, w, rows_eff, P.part);
+  if (!grid_barrier(gs, okflag)) return -1;
+  reduce_partials(P.part, E, 1, E, put);
+  if (!grid_barrier(gs, okflag)) return -1;
+  wide_load_gram(P.red, w, S.M, S.gd, false);
+  __syncthreads();
+  chol_cta(S.M, MS, w, S.gd, 1e-4f, S.wrinv, &S.wok);
+  if (!S.wok) return 0;
+  wide_solve(S.X, w, rows, rows_eff, S.M, S.wrinv, S.Rt);
+  // ---- pass 2: G2 = X^T X = I + E into M's upper triangle (L stays below)
+  wide_gram(S.X, w, rows_eff, P.part);
+  if (!grid_barrier(gs, okflag)) return -1;
+  reduce_partials(P.part, E, 1, E, put);
+  if (!grid_barrier(gs, okflag)) return -1;
+  wide_load_gram(P.red, w, S.M, S.gd, true);
+  __syncthreads();
+  if (tid < 32) {  // first order only when max |E| <= 3e-4
+    float dev = 0.f;
+    for (int i = tid; i < w; i += 32) {
+      dev = fmaxf(dev, fabsf(S.gd[i] - 1.f));
+      for (int j = i + 1; j < w; ++j) dev = fmaxf(dev, fabsf(S.M[i * MS + j]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dev = fmaxf(dev, __shfl_xor_sync(0xffffffffu, dev, o));
+    if (tid == 0) S.wok = dev <= 3e-4f ? 1 : 0;
+  }
+  __syncthreads();
+  if (!S.wok) return 0;
+  for (int i = tid; i < w; i += LT) S.gd[i] = 0.5f * (S.gd[i] - 1.f);  // F's diagonal
+  __syncthreads();
+  // ---- Q = X (I - F); R = (I + F) R1
+  wide_apply_f(S.X, w, rows, rows_eff, S.M, S.gd, S.Rt);
+  // R = (I + F) R1: every CTA holds the same L and F, so column j of R is formed
+  // by CTA j mod grid, one row per thread (R1[l][j] = L[j][l] is row j of M)
+  for (int j = blockIdx.x; j < w; j += gridDim.x) {
+    for (int i = tid; i < w; i += LT) {
+      float sum = 0.f;
+      if (i <= j) {
+        sum = S.M[j * MS + i];  // R1[i][j]
+        sum = fmaf(S.gd[i], S.M[j * MS + i], sum);
+        for (int l = i + 1; l <= j; ++l) sum = fmaf(S.M[i * MS + l], S.M[j * MS + l], sum);
+      }
+      P.R[i + static_cast<int64_t>(j) * P.ldr] = sum;
+    }
+  }
+  __syncthreads();
+  return 1;
+}
+
 __global__ void __launch_bounds__(LT, 1) leaf_res_kernel(LeafPlan P) {
   extern __shared__ __align__(16) unsigned char smraw[];
   ResSmem& S = *reinterpret_cast<ResSmem*>(smraw);
@@ -934,7 +1213,17 @@ __global__ void __launch_bounds__(LT, 1) leaf_res_kernel(LeafPlan P) {
   res_load(P, S.X, r0, rows, P.w);
   __syncthreads();
   bool ok = true;
-  for (int i = 0; i < P.nsteps && ok; ++i) {
+  int done = 0;
+  if (P.wide) {
+    done = res_wide(P, S, gs, &okflag, rows);
+    if (done < 0) ok = false;
+    if (done == 0) {  // not conditioned well enough for one CholQR2 over the leaf: 32-column panels
+      __syncthreads();
+      res_load(P, S.X, r0, rows, P.w);
+      __syncthreads();
+    }
+  }
+  for (int i = 0; i < P.nsteps && ok && !done; ++i) {
     const LeafStep s = P.step[i];
     __syncthreads();
     if (s.kind == 0) {
@@ -1058,8 +1347,8 @@ int64_t leaf_fused_work(int m) {
 }
 
 later_status_t leaf_fused(cudaStream_t st, int m, int w, float* A, int64_t lda, float* R, int64_t ldr, void* qh,
-                          void* ql, int64_t ldh, int out_prec, int cgs2, Arena& ws, int* sync, int* tsqr_counters,
-                          long long budget, int* fallbacks) {
+                          void* ql, int64_t ldh, int out_prec, int cgs2, bool try_wide, Arena& ws, int* sync,
+                          int* tsqr_counters, long long budget, int* fallbacks) {
   if (w < 1 || w > kLeafMaxWidth || m < w) return LATER_ERR_INVALID_ARG;
   int res_rpc = 0;
   const int res_grid = leaf_res_grid(m, &res_rpc);
@@ -1071,6 +1360,8 @@ later_status_t leaf_fused(cudaStream_t st, int m, int w, float* A, int64_t lda, 
   P.w = w;
   P.rpc = resident ? res_rpc : (m + grid - 1) / grid;
   P.vec = (reinterpret_cast<uintptr_t>(A) % 16 == 0) && (lda % 4 == 0);
+  // one CholQR2 over the whole leaf first (resident slabs, wider than one panel, no CGS2 requested)
+  P.wide = try_wide && resident && w > 32 && !cgs2;
   P.cgs2 = cgs2;
   P.mode = out_prec == LATER_PREC_BF16 ? 1 : (out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
   build_steps(w, 0, &P);

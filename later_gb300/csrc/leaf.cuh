@@ -27,7 +27,7 @@ int64_t leaf_fused_work(int m);
 // Returns LATER_ERR_NOT_SUPPORTED when the device cannot run the cooperative
 // launch (the caller then uses the multi-launch leaf).
 later_status_t leaf_fused(cudaStream_t st, int m, int w, float* A, int64_t lda, float* R, int64_t ldr, void* qh,
-                          void* ql, int64_t ldh, int out_prec, int cgs2, Arena& ws, int* sync, int* tsqr_counters,
-                          long long budget, int* fallbacks);
+                          void* ql, int64_t ldh, int out_prec, int cgs2, bool try_wide, Arena& ws, int* sync,
+                          int* tsqr_counters, long long budget, int* fallbacks);
 
 }  // namespace later

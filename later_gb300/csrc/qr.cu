@@ -92,10 +92,10 @@ later_status_t leaf_qr(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t l
 // A leaf: one fused launch (leaf.cu) unless the caller asked for the
 // reference's panel algorithm or the device / workspace cannot run it.
 later_status_t leaf_top(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
-  if (c.o.panel == 0 && w <= kLeafMaxWidth) {
+  if ((c.o.panel == 0 || c.o.panel == 2) && w <= kLeafMaxWidth) {
     const later_status_t s =
         leaf_fused(c.st, c.m, w, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
-                   c.o.prec, c.o.cgs2, *c.ws, c.counters + 4096, c.counters, c.o.budget, nullptr);
+                   c.o.prec, c.o.cgs2, c.o.panel == 2, *c.ws, c.counters + 4096, c.counters, c.o.budget, nullptr);
     if (s != LATER_ERR_NOT_SUPPORTED && s != LATER_ERR_WORKSPACE) return s;
   }
   return leaf_qr(c, w, A, lda, R, ldr, col);

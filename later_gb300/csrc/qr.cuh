@@ -10,7 +10,7 @@ struct Options {
   int prec = LATER_PREC_FP16;
   int cgs2 = 0;
   int leaf = 128;
-  int panel = 0;  // 0: fused CholQR2 leaf (MGS-TSQR fallback); 1: MGS-TSQR panels, separate launches
+  int panel = 0;  // 0: fused leaf, 32-column CholQR2 panels; 2: fused, leaf-wide CholQR2 first; 1: MGS-TSQR
   long long budget = kDefaultBudgetCycles;
 };
 

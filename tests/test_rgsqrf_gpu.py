@@ -130,3 +130,27 @@ def test_fused_leaf_falls_back_on_dependent_columns(cuda):
     # Panel 0 was factored by the fallback: the same MGS-TSQR arithmetic as the reference's path,
     # bit for bit (CholQR2 would round differently).
     assert np.array_equal(Qf[:, :32], Qm[:, :32]) and np.array_equal(Rf[:32, :32], Rm[:32, :32])
+
+
+@pytest.mark.parametrize("m,n,prec", [(4096, 512, "fp16"), (2048, 256, "split3"), (16384, 128, "fp16"), (1000, 200, "bf16")])
+def test_wide_leaf_matches_mgs_panels(cuda, m, n, prec):
+    """panel = 2: one CholQR2 over each whole leaf when it is well conditioned (else 32-column
+    panels): same factorisation as the reference's panel algorithm to working accuracy."""
+    A = gen.normal(m, n, seed=5 + n)
+    Qw, Rw = run_gpu(A, precision=prec, panel="wide")
+    Qm, Rm = run_gpu(A, precision=prec, panel="mgs")
+    assert metrics.qr_backward_error(A, Qw, Rw) <= BOUND_BWD[prec]
+    assert np.all(np.tril(Rw, -1) == 0) and np.all(np.diag(Rw) > 0)
+    assert np.linalg.norm(Rw - Rm) / np.linalg.norm(Rm) <= 2 * BOUND_BWD[prec]
+    assert metrics.orthogonality(Qw) <= 2 * metrics.orthogonality(Qm) + 1e-5
+
+
+def test_wide_leaf_falls_back_on_dependent_columns(cuda):
+    """With exactly dependent columns the leaf-wide factorisation is refused and the leaf falls
+    back to 32-column panels and, for the affected panel, to MGS-TSQR."""
+    A = gen.normal(2048, 128, seed=11)
+    A[:, 5] = A[:, 3]
+    Qw, Rw = run_gpu(A, panel="wide")
+    Qm, Rm = run_gpu(A, panel="mgs")
+    assert np.all(np.isfinite(Qw)) and metrics.qr_backward_error(A, Qw, Rw) <= BOUND_BWD["fp16"]
+    assert np.array_equal(Qw[:, :32], Qm[:, :32]) and np.array_equal(Rw[:32, :32], Rm[:32, :32])
