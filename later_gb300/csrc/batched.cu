@@ -44,17 +44,72 @@ struct Item {
   int pad;
 };
 
+// Shared tiles are column-major (column c at c * (CR + 4)) so that four
+// consecutive rows of a column are one float4.
 template <int CR>
 struct Smem {
-  float q[CR][NMAX - PW + 1];  // chunk of the previous Q columns (up to 224)
-  float a[CR][PW + 1];         // chunk of the current panel
-  float c[NMAX - PW][PW + 1];  // projection coefficients
-  float g[PW][PW + 1];         // Gram matrix / Cholesky factor
+  static constexpr int LD = CR + 4;
+  float q[(NMAX - PW) * LD];  // chunk of the previous Q columns (up to 224)
+  float a[PW * LD];           // chunk of the current panel
+  float c[(NMAX - PW) * (PW + 1)];  // projection coefficients C[i][j]
+  float g[PW][PW + 1];              // Gram matrix / Cholesky factor
+  float ginv[PW];                   // reciprocals of the factor's diagonal
+  float red[8 * PW * PW];           // per-warp partial sums of a Gram matrix
 };
 
-// C[i][j] = sum_r Q[r][i] A[r][j] over all m rows (i < k1, j < w).
+// Stages rows [r0, r0 + rows) of columns [c0, c0 + nc) into dst (column-major,
+// stride LD), rows beyond `rows` (up to the next multiple of 4) as zeros.
+// Global reads are issued eight per thread before the shared-memory stores
+// (float4 along rows when the matrix allows it), so a chunk costs a few memory
+// latencies rather than one per element.
+template <int CR>
+__device__ void stage(float* dst, const Item& it, int r0, int rows, int c0, int nc) {
+  const int LD = CR + 4;
+  const int rq = (rows + 3) & ~3;
+  const bool vec = rows == rq && (it.lda % 4 == 0) && (reinterpret_cast<uintptr_t>(it.A) % 16 == 0);
+  if (vec) {  // r0 is a multiple of CR, so every float4 is aligned
+    const int nq = rq / 4, total = nq * nc;
+    for (int base = threadIdx.x; base < total; base += 8 * THREADS) {
+      float4 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * THREADS;
+        v[u] = e < total ? *reinterpret_cast<const float4*>(it.A + r0 + 4 * (e % nq) +
+                                                             static_cast<int64_t>(c0 + e / nq) * it.lda)
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = base + u * THREADS;
+        if (e < total) *reinterpret_cast<float4*>(&dst[(e / nq) * LD + 4 * (e % nq)]) = v[u];
+      }
+    }
+    return;
+  }
+  const int total = rq * nc;
+  for (int base = threadIdx.x; base < total; base += 8 * THREADS) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * THREADS;
+      const int r = e % rq, c = e / rq;
+      v[u] = (e < total && r < rows) ? it.A[r0 + r + static_cast<int64_t>(c0 + c) * it.lda] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * THREADS;
+      if (e < total) dst[(e / rq) * LD + e % rq] = v[u];
+    }
+  }
+}
+
+// C[i][j] = sum_r Q[r][i] A[r][j] over all m rows (i < k1, j < w). Thread
+// (j = t % 32, i0 = t / 32) owns C[i0 + 8u][j]; four rows per step, the Q column
+// read as one float4 (the same for the whole warp: a broadcast) and the A column
+// as one float4.
 template <int CR>
 __device__ void project(Smem<CR>& s, const Item& it, int c0, int w, int k1) {
+  const int LD = CR + 4;
   const int t = threadIdx.x;
   const int j = t % PW, i0 = t / PW;  // i = i0 + 8 u
   float acc[(NMAX - PW) / 8];
@@ -63,76 +118,108 @@ __device__ void project(Smem<CR>& s, const Item& it, int c0, int w, int k1) {
   for (int r0 = 0; r0 < it.m; r0 += CR) {
     const int rows = min(CR, it.m - r0);
     __syncthreads();
-    for (int e = t; e < CR * k1; e += THREADS) {
-      const int r = e % CR, i = e / CR;
-      s.q[r][i] = r < rows ? it.A[r0 + r + static_cast<int64_t>(i) * it.lda] : 0.f;
-    }
-    for (int e = t; e < CR * PW; e += THREADS) {
-      const int r = e % CR, jj = e / CR;
-      s.a[r][jj] = (r < rows && jj < w) ? it.A[r0 + r + static_cast<int64_t>(c0 + jj) * it.lda] : 0.f;
-    }
+    stage<CR>(s.q, it, r0, rows, 0, k1);
+    stage<CR>(s.a, it, r0, rows, c0, w);
     __syncthreads();
-    for (int r = 0; r < rows; ++r) {
-      const float av = s.a[r][j];
+    const int rq = (rows + 3) & ~3;
+    for (int r = 0; r < rq; r += 4) {
+      const float4 av = *reinterpret_cast<const float4*>(&s.a[j * LD + r]);
 #pragma unroll
-      for (int u = 0; u < (NMAX - PW) / 8; ++u)
-        if (i0 + 8 * u < k1) acc[u] += s.q[r][i0 + 8 * u] * av;
+      for (int u = 0; u < (NMAX - PW) / 8; ++u) {
+        if (i0 + 8 * u < k1) {
+          const float4 qv = *reinterpret_cast<const float4*>(&s.q[(i0 + 8 * u) * LD + r]);
+          acc[u] = fmaf(qv.w, av.w, fmaf(qv.z, av.z, fmaf(qv.y, av.y, fmaf(qv.x, av.x, acc[u]))));
+        }
+      }
     }
   }
   __syncthreads();
 #pragma unroll
   for (int u = 0; u < (NMAX - PW) / 8; ++u)
-    if (i0 + 8 * u < k1) s.c[i0 + 8 * u][j] = acc[u];
+    if (i0 + 8 * u < k1) s.c[(i0 + 8 * u) * (PW + 1) + j] = (j < w) ? acc[u] : 0.f;
   __syncthreads();
 }
 
-// A_p -= Q_<p C.
+// A_p -= Q_<p C, chunk by chunk: each thread updates a 4-row x 2-column tile of
+// the staged panel chunk, reading Q as float4 along rows.
 template <int CR>
 __device__ void subtract(Smem<CR>& s, const Item& it, int c0, int w, int k1) {
+  const int LD = CR + 4;
   const int t = threadIdx.x;
   for (int r0 = 0; r0 < it.m; r0 += CR) {
     const int rows = min(CR, it.m - r0);
+    const int rq = (rows + 3) & ~3;
     __syncthreads();
-    for (int e = t; e < CR * k1; e += THREADS) {
-      const int r = e % CR, i = e / CR;
-      s.q[r][i] = r < rows ? it.A[r0 + r + static_cast<int64_t>(i) * it.lda] : 0.f;
+    stage<CR>(s.q, it, r0, rows, 0, k1);
+    stage<CR>(s.a, it, r0, rows, c0, w);
+    __syncthreads();
+    const int ntile = (rq / 4) * (PW / 2);
+    for (int e = t; e < ntile; e += THREADS) {
+      const int rt = e % (rq / 4), ct = e / (rq / 4);
+      const int r = 4 * rt, jj = 2 * ct;
+      float4 x0 = *reinterpret_cast<const float4*>(&s.a[jj * LD + r]);
+      float4 x1 = *reinterpret_cast<const float4*>(&s.a[(jj + 1) * LD + r]);
+      for (int i = 0; i < k1; ++i) {
+        const float4 qv = *reinterpret_cast<const float4*>(&s.q[i * LD + r]);
+        const float c0v = s.c[i * (PW + 1) + jj], c1v = s.c[i * (PW + 1) + jj + 1];
+        x0.x = fmaf(-qv.x, c0v, x0.x); x0.y = fmaf(-qv.y, c0v, x0.y);
+        x0.z = fmaf(-qv.z, c0v, x0.z); x0.w = fmaf(-qv.w, c0v, x0.w);
+        x1.x = fmaf(-qv.x, c1v, x1.x); x1.y = fmaf(-qv.y, c1v, x1.y);
+        x1.z = fmaf(-qv.z, c1v, x1.z); x1.w = fmaf(-qv.w, c1v, x1.w);
+      }
+      *reinterpret_cast<float4*>(&s.a[jj * LD + r]) = x0;
+      *reinterpret_cast<float4*>(&s.a[(jj + 1) * LD + r]) = x1;
     }
     __syncthreads();
-    for (int e = t; e < CR * PW; e += THREADS) {
-      const int r = e % CR, jj = e / CR;
-      if (r >= rows || jj >= w) continue;
-      float* p = &it.A[r0 + r + static_cast<int64_t>(c0 + jj) * it.lda];
-      float v = *p;
-      for (int i = 0; i < k1; ++i) v -= s.q[r][i] * s.c[i][jj];
-      *p = v;
+    for (int e = t; e < rows * w; e += THREADS) {
+      const int r = e % rows, jj = e / rows;
+      it.A[r0 + r + static_cast<int64_t>(c0 + jj) * it.lda] = s.a[jj * LD + r];
     }
   }
   __syncthreads();
 }
 
-// G = A_p^T A_p (w x w, stored in s.g).
+// G = A_p^T A_p (w x w, into s.g): warp wp takes rows 4 wp, 4 wp + 32, ... of
+// each chunk; lane (i = l / 4 .. ) owns 4 x 8 entries; warp partials are added
+// in warp order.
 template <int CR>
 __device__ void gram(Smem<CR>& s, const Item& it, int c0, int w) {
+  const int LD = CR + 4;
   const int t = threadIdx.x;
-  const int j = t % PW, i0 = t / PW;  // i = i0 + 8 u, u < 4
-  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const int lane = t % 32, wp = t / 32;
+  const int ti = lane % 8, tj = lane / 8;  // entries (ti + 8 u, tj + 4 v), u < 4, v < 8
+  float acc[4][8] = {};
   for (int r0 = 0; r0 < it.m; r0 += CR) {
     const int rows = min(CR, it.m - r0);
+    const int rq = (rows + 3) & ~3;
     __syncthreads();
-    for (int e = t; e < CR * PW; e += THREADS) {
-      const int r = e % CR, jj = e / CR;
-      s.a[r][jj] = (r < rows && jj < w) ? it.A[r0 + r + static_cast<int64_t>(c0 + jj) * it.lda] : 0.f;
-    }
+    stage<CR>(s.a, it, r0, rows, c0, w);
     __syncthreads();
-    for (int r = 0; r < rows; ++r) {
-      const float av = s.a[r][j];
+    for (int r = 4 * wp; r < rq; r += 32) {
+      float4 x[4], y[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) acc[u] += s.a[r][i0 + 8 * u] * av;
+      for (int u = 0; u < 4; ++u) x[u] = *reinterpret_cast<const float4*>(&s.a[(ti + 8 * u) * LD + r]);
+#pragma unroll
+      for (int v = 0; v < 8; ++v) y[v] = *reinterpret_cast<const float4*>(&s.a[(tj + 4 * v) * LD + r]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v)
+          acc[u][v] = fmaf(x[u].w, y[v].w, fmaf(x[u].z, y[v].z, fmaf(x[u].y, y[v].y, fmaf(x[u].x, y[v].x, acc[u][v]))));
     }
   }
-  __syncthreads();
 #pragma unroll
-  for (int u = 0; u < 4; ++u) s.g[i0 + 8 * u][j] = acc[u];
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) s.red[wp * PW * PW + (ti + 8 * u) * PW + tj + 4 * v] = acc[u][v];
+  __syncthreads();
+  for (int e = t; e < PW * PW; e += THREADS) {
+    float v = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v += s.red[q * PW * PW + e];
+    const int i = e / PW, j = e % PW;
+    s.g[i][j] = (i < w && j < w) ? v : 0.f;
+  }
   __syncthreads();
 }
 
@@ -152,7 +239,10 @@ __device__ bool chol(Smem<CR>& s, int w) {
       }
       const float piv = sqrtf(d);
       __syncwarp();
-      if (l == k) s.g[k][k] = piv;
+      if (l == k) {
+        s.g[k][k] = piv;
+        s.ginv[k] = 1.f / piv;
+      }
       if (l > k && l < w) s.g[l][k] /= piv;
       __syncwarp();
       if (l > k && l < w)
@@ -174,11 +264,10 @@ __device__ void trsm_rows(Smem<CR>& s, const Item& it, int c0, int w) {
 #pragma unroll
     for (int j = 0; j < PW; ++j) {
       if (j < w) {
-        float v = x[j];
+        x[j] *= s.ginv[j];
 #pragma unroll
-        for (int i = 0; i < PW; ++i)
-          if (i < j) v -= x[i] * s.g[j][i];
-        x[j] = v / s.g[j][j];
+        for (int i = j + 1; i < PW; ++i)
+          if (i < w) x[i] = fmaf(-x[j], s.g[i][j], x[i]);
       }
     }
 #pragma unroll
@@ -189,7 +278,7 @@ __device__ void trsm_rows(Smem<CR>& s, const Item& it, int c0, int w) {
 }
 
 template <int CR>
-__global__ void __launch_bounds__(THREADS) batched_qr_kernel(const Item* items, int count, int* queue, int* status) {
+__global__ void __launch_bounds__(THREADS, 1) batched_qr_kernel(const Item* items, int count, int* queue, int* status) {
   extern __shared__ float smraw[];
   Smem<CR>& s = *reinterpret_cast<Smem<CR>*>(smraw);
   __shared__ int cur;
@@ -214,7 +303,7 @@ __global__ void __launch_bounds__(THREADS) batched_qr_kernel(const Item* items, 
           for (int e = threadIdx.x; e < c0 * w; e += THREADS) {
             const int i = e % c0, j = e / c0;
             float* rp = &it.R[i + static_cast<int64_t>(c0 + j) * it.ldr];
-            *rp = (pass ? *rp : 0.f) + s.c[i][j];
+            *rp = (pass ? *rp : 0.f) + s.c[i * (PW + 1) + j];
           }
           subtract(s, it, c0, w, c0);
         }

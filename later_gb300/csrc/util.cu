@@ -99,9 +99,12 @@ __global__ void convert_kernel(int m, int n, const float* __restrict__ A, int64_
   }
 }
 
+// Each block covers 256 rows and only visits the columns left of its last row
+// (the rest of its column range lies on or above the diagonal).
 __global__ void fill_strict_lower_kernel(int m, int n, float* A, int64_t lda, float v) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int j = blockIdx.y; j < n; j += gridDim.y)
+  const int jend = min(n, static_cast<int>(blockIdx.x * blockDim.x + blockDim.x));
+  for (int j = blockIdx.y; j < jend; j += gridDim.y)
     if (i < m && i > j) A[i + static_cast<int64_t>(j) * lda] = v;
 }
 
@@ -136,7 +139,8 @@ inline dim3 grid2d(int m, int n) {
 later_status_t fill_strict_lower(cudaStream_t st, int m, int n, float* A, int64_t lda, float v) {
   if (m <= 0 || n <= 0) return LATER_OK;
   TraceScope trace(st, TRACE_OTHER);
-  fill_strict_lower_kernel<<<grid2d(m, n), 256, 0, st>>>(m, n, A, lda, v);
+  fill_strict_lower_kernel<<<dim3(static_cast<unsigned>((m + 255) / 256), static_cast<unsigned>(n < 512 ? n : 512)), 256,
+                             0, st>>>(m, n, A, lda, v);
   note_launch();
   return cuda_status(cudaGetLastError());
 }
