@@ -25,6 +25,7 @@
 #include <algorithm>
 
 #include "blas3.cuh"
+#include "dense_dev.cuh"
 #include "panel.cuh"
 #include "runtime.cuh"
 
@@ -357,91 +358,51 @@ __global__ void __launch_bounds__(256) trmm_leaf(int nb, int n, const float* __r
 
 // Lower Cholesky of an nb x nb block (nb <= 128) in one CTA, in shared memory
 // (column-major, stride LDL), right-looking over 32-column blocks. Warp 0
-// factors the 32 x 32 diagonal block with lane = row in registers: per pivot
-// one IEEE square root and one reciprocal (the column is scaled by it, as
-// LAPACK's spotf2 does), the scaled column broadcast through shared memory as
-// float4. One thread per row then solves the block column below the diagonal
-// block, and the CTA updates the trailing lower triangle in 4 x 4 register
-// tiles. A non-positive (or NaN) pivot sets DEV_NUMERIC and the factorisation
-// continues with pivot 1 so the kernel always finishes.
+// factors the 32 x 32 diagonal block with the compact register-window
+// Cholesky (dense_dev.cuh; pivots d * rsqrt(d)), one thread per row solves the
+// block column below it with the blocked row substitution, and the CTA
+// updates the trailing lower triangle in 4 x 4 register tiles. A non-positive
+// (or NaN) pivot sets DEV_NUMERIC; the factorisation continues (with pivot 1)
+// so the kernel always finishes.
+struct PotrfSmem {
+  float G[32 * 33];   // the diagonal block, row-major
+  float Rc[32 * RCS]; // its factor, column-major R = L^T
+  float rinv[32];
+  int ok;
+};
+
 __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda, int* status) {
   extern __shared__ __align__(16) float sm[];
-  float* Ac = sm;                // A[i][j] at j*LDL + i (lower triangle used)
-  float* col = sm + LDL * NB;    // 32 floats: broadcast column
-  float* rdiag = col + 32;       // 32 floats: reciprocals of the block's pivots
+  float* Ac = sm;  // A[i][j] at j*LDL + i (lower triangle used)
+  PotrfSmem& ps = *reinterpret_cast<PotrfSmem*>(sm + LDL * NB);
   stage_cols(nb, A, lda, Ac, LDL);
   __syncthreads();
-  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  const int tid = threadIdx.x;
+  bool bad = false;
   for (int k0 = 0; k0 < nb; k0 += 32) {
     const int kb = min(32, nb - k0);
-    if (warp == 0) {
-      float d[32];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) d[j] = (lane < kb && j <= lane) ? Ac[(k0 + j) * LDL + k0 + lane] : 0.f;
-      bool bad = false;
-#pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        if (k < kb) {
-          float dk = __shfl_sync(0xffffffffu, d[k], k);
-          if (!(dk > 0.f)) {
-            bad = true;
-            dk = 1.f;
-          }
-          const float piv = sqrtf(dk);
-          const float rinv = 1.f / piv;
-          if (lane == k) {
-            d[k] = piv;
-            rdiag[k] = rinv;
-          }
-          if (lane > k) d[k] *= rinv;
-          col[lane] = d[k];
-          __syncwarp();
-#pragma unroll
-          for (int jq = (k + 1) / 4; jq < 8; ++jq) {
-            const float4 c4 = reinterpret_cast<const float4*>(col)[jq];
-            const float cv[4] = {c4.x, c4.y, c4.z, c4.w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const int j = 4 * jq + e;
-              if (j > k && lane >= j) d[j] -= d[k] * cv[e];
-            }
-          }
-          __syncwarp();
-        }
-      }
-      if (bad && lane == 0) report(status, DEV_NUMERIC);
-      if (lane < kb) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (j <= lane) Ac[(k0 + j) * LDL + k0 + lane] = d[j];
-      }
+    for (int e = tid; e < 32 * 32; e += blockDim.x) {
+      const int i = e / 32, j = e % 32;
+      ps.G[i * 33 + j] = (i < kb && j < kb && j <= i) ? Ac[(k0 + j) * LDL + k0 + i] : 0.f;
     }
     __syncthreads();
-    // rows below the diagonal block: x D^T = a (D = L[k0.., k0..], kb x kb)
-    const int t0 = k0 + kb;
-    for (int r = t0 + threadIdx.x; r < nb; r += blockDim.x) {
-      float x[32];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) x[j] = j < kb ? Ac[(k0 + j) * LDL + r] : 0.f;
-#pragma unroll
-      for (int l = 0; l < 32; ++l) {
-        if (l < kb) {
-          x[l] *= rdiag[l];
-          const float* dcol = Ac + (k0 + l) * LDL + k0;  // column l of D
-#pragma unroll
-          for (int j = l + 1; j < 32; ++j) x[j] -= x[l] * dcol[j];
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (j < kb) Ac[(k0 + j) * LDL + r] = x[j];
+    chol_upper(ps.G, kb, ps.Rc, ps.rinv, false, &ps.ok, 0.f);
+    __syncthreads();
+    if (!ps.ok) bad = true;
+    // the factor back into the block: L[i][j] = R[j][i] = Rc[i * RCS + j]
+    for (int e = tid; e < kb * kb; e += blockDim.x) {
+      const int i = e % kb, j = e / kb;
+      if (j <= i) Ac[(k0 + j) * LDL + k0 + i] = ps.Rc[i * RCS + j];
     }
+    // rows below the diagonal block: x R = a with R = L_D^T
+    const int t0 = k0 + kb;
+    for (int r = t0 + tid; r < nb; r += blockDim.x) rows_solve(Ac + k0 * LDL, LDL, kb, r, ps.Rc, ps.rinv);
     __syncthreads();
     // trailing lower triangle: A[i][j] -= sum_l A[i][k0+l] A[j][k0+l], i >= j >= t0
     const int t = nb - t0;
     const int nt = (t + 3) / 4;
     const int ntiles = nt * (nt + 1) / 2;
-    for (int q = threadIdx.x; q < ntiles; q += blockDim.x) {
+    for (int q = tid; q < ntiles; q += blockDim.x) {
       int ti = static_cast<int>((sqrtf(8.f * q + 1.f) - 1.f) * 0.5f);
       while (ti * (ti + 1) / 2 > q) --ti;
       while ((ti + 1) * (ti + 2) / 2 <= q) ++ti;
@@ -457,7 +418,7 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
-          for (int v = 0; v < 4; ++v) acc[u][v] += av[u] * bv[v];
+          for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u)
@@ -469,7 +430,8 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
     }
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+  if (bad && tid == 0) report(status, DEV_NUMERIC);
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
     const int i = e % nb, j = e / nb;
     if (i >= j) A[i + static_cast<int64_t>(j) * lda] = Ac[j * LDL + i];
   }
@@ -684,7 +646,7 @@ later_status_t trmm_rec(B3& b, int m, int n, const float* L, int64_t ldl, const 
 
 later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda) {
   if (n <= NB) {
-    const size_t smem = (NB * LDL + 64) * sizeof(float);
+    const size_t smem = NB * LDL * sizeof(float) + sizeof(PotrfSmem);
     if (!smem_attr(reinterpret_cast<const void*>(potrf_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_PANEL);
     potrf_leaf<<<1, 256, smem, b.st>>>(n, A, lda, device_status_ptr());
