@@ -13,8 +13,8 @@
 //     CholQR2 inside the panel: G = A_p^T A_p, G = L L^T (one warp),
 //            A_p <- A_p L^-T   (twice; R[p, p] = L2^T L1^T)
 // Every product streams the matrix through shared memory in row chunks of
-// CR rows (the tunable tile), so the work is throughput- not latency-bound and
-// needs no inter-CTA communication. All arithmetic is FP32; reductions run in
+// CR rows (the tunable tile), five streams per panel with the products that
+// share a chunk fused, and needs no inter-CTA communication. All arithmetic is FP32; reductions run in
 // a fixed order (deterministic). A Cholesky pivot <= 0 (a rank-deficient or
 // very ill-conditioned panel: CholQR2 needs kappa(panel) below about 1e3 in
 // FP32) marks that matrix's status as LATER_ERR_NUMERIC.
@@ -103,117 +103,92 @@ __device__ void stage(float* dst, const Item& it, int r0, int rows, int c0, int 
   }
 }
 
-// C[i][j] = sum_r Q[r][i] A[r][j] over all m rows (i < k1, j < w). Thread
-// (j = t % 32, i0 = t / 32) owns C[i0 + 8u][j]; four rows per step, the Q column
-// read as one float4 (the same for the whole warp: a broadcast) and the A column
-// as one float4.
+// ---- chunk-level pieces (the staged chunk: Q columns in s.q, the panel in s.a)
+
+// acc[u] += sum over the chunk's rows of Q[r][i0 + 8u] A[r][j] (thread j = t % 32,
+// i0 = t / 32): the Q column read as one float4 (the same for the whole warp: a
+// broadcast), the A column as one float4.
 template <int CR>
-__device__ void project(Smem<CR>& s, const Item& it, int c0, int w, int k1) {
+__device__ __forceinline__ void chunk_project(const Smem<CR>& s, int rq, int k1, float (&acc)[(NMAX - PW) / 8]) {
   const int LD = CR + 4;
-  const int t = threadIdx.x;
-  const int j = t % PW, i0 = t / PW;  // i = i0 + 8 u
-  float acc[(NMAX - PW) / 8];
+  const int j = threadIdx.x % PW, i0 = threadIdx.x / PW;
+  for (int r = 0; r < rq; r += 4) {
+    const float4 av = *reinterpret_cast<const float4*>(&s.a[j * LD + r]);
 #pragma unroll
-  for (int u = 0; u < (NMAX - PW) / 8; ++u) acc[u] = 0.f;
-  for (int r0 = 0; r0 < it.m; r0 += CR) {
-    const int rows = min(CR, it.m - r0);
-    __syncthreads();
-    stage<CR>(s.q, it, r0, rows, 0, k1);
-    stage<CR>(s.a, it, r0, rows, c0, w);
-    __syncthreads();
-    const int rq = (rows + 3) & ~3;
-    for (int r = 0; r < rq; r += 4) {
-      const float4 av = *reinterpret_cast<const float4*>(&s.a[j * LD + r]);
-#pragma unroll
-      for (int u = 0; u < (NMAX - PW) / 8; ++u) {
-        if (i0 + 8 * u < k1) {
-          const float4 qv = *reinterpret_cast<const float4*>(&s.q[(i0 + 8 * u) * LD + r]);
-          acc[u] = fmaf(qv.w, av.w, fmaf(qv.z, av.z, fmaf(qv.y, av.y, fmaf(qv.x, av.x, acc[u]))));
-        }
+    for (int u = 0; u < (NMAX - PW) / 8; ++u) {
+      if (i0 + 8 * u < k1) {
+        const float4 qv = *reinterpret_cast<const float4*>(&s.q[(i0 + 8 * u) * LD + r]);
+        acc[u] = fmaf(qv.w, av.w, fmaf(qv.z, av.z, fmaf(qv.y, av.y, fmaf(qv.x, av.x, acc[u]))));
       }
     }
   }
-  __syncthreads();
+}
+
+// C (k1 x w) from the projection accumulators into s.c (zeros for j >= w).
+template <int CR>
+__device__ __forceinline__ void store_projection(Smem<CR>& s, int k1, int w, const float (&acc)[(NMAX - PW) / 8]) {
+  const int j = threadIdx.x % PW, i0 = threadIdx.x / PW;
 #pragma unroll
   for (int u = 0; u < (NMAX - PW) / 8; ++u)
     if (i0 + 8 * u < k1) s.c[(i0 + 8 * u) * (PW + 1) + j] = (j < w) ? acc[u] : 0.f;
-  __syncthreads();
 }
 
-// A_p -= Q_<p C, chunk by chunk: each thread updates a 4-row x 2-column tile of
-// the staged panel chunk, reading Q as float4 along rows.
+// The staged panel chunk -= Q C (C in s.c): each thread updates a 4-row x
+// 2-column tile, reading Q as float4 along rows.
 template <int CR>
-__device__ void subtract(Smem<CR>& s, const Item& it, int c0, int w, int k1) {
+__device__ __forceinline__ void chunk_subtract(Smem<CR>& s, int rq, int k1) {
   const int LD = CR + 4;
-  const int t = threadIdx.x;
-  for (int r0 = 0; r0 < it.m; r0 += CR) {
-    const int rows = min(CR, it.m - r0);
-    const int rq = (rows + 3) & ~3;
-    __syncthreads();
-    stage<CR>(s.q, it, r0, rows, 0, k1);
-    stage<CR>(s.a, it, r0, rows, c0, w);
-    __syncthreads();
-    const int ntile = (rq / 4) * (PW / 2);
-    for (int e = t; e < ntile; e += THREADS) {
-      const int rt = e % (rq / 4), ct = e / (rq / 4);
-      const int r = 4 * rt, jj = 2 * ct;
-      float4 x0 = *reinterpret_cast<const float4*>(&s.a[jj * LD + r]);
-      float4 x1 = *reinterpret_cast<const float4*>(&s.a[(jj + 1) * LD + r]);
-      for (int i = 0; i < k1; ++i) {
-        const float4 qv = *reinterpret_cast<const float4*>(&s.q[i * LD + r]);
-        const float c0v = s.c[i * (PW + 1) + jj], c1v = s.c[i * (PW + 1) + jj + 1];
-        x0.x = fmaf(-qv.x, c0v, x0.x); x0.y = fmaf(-qv.y, c0v, x0.y);
-        x0.z = fmaf(-qv.z, c0v, x0.z); x0.w = fmaf(-qv.w, c0v, x0.w);
-        x1.x = fmaf(-qv.x, c1v, x1.x); x1.y = fmaf(-qv.y, c1v, x1.y);
-        x1.z = fmaf(-qv.z, c1v, x1.z); x1.w = fmaf(-qv.w, c1v, x1.w);
-      }
-      *reinterpret_cast<float4*>(&s.a[jj * LD + r]) = x0;
-      *reinterpret_cast<float4*>(&s.a[(jj + 1) * LD + r]) = x1;
+  const int ntile = (rq / 4) * (PW / 2);
+  for (int e = threadIdx.x; e < ntile; e += THREADS) {
+    const int rt = e % (rq / 4), ct = e / (rq / 4);
+    const int r = 4 * rt, jj = 2 * ct;
+    float4 x0 = *reinterpret_cast<const float4*>(&s.a[jj * LD + r]);
+    float4 x1 = *reinterpret_cast<const float4*>(&s.a[(jj + 1) * LD + r]);
+    for (int i = 0; i < k1; ++i) {
+      const float4 qv = *reinterpret_cast<const float4*>(&s.q[i * LD + r]);
+      const float c0v = s.c[i * (PW + 1) + jj], c1v = s.c[i * (PW + 1) + jj + 1];
+      x0.x = fmaf(-qv.x, c0v, x0.x); x0.y = fmaf(-qv.y, c0v, x0.y);
+      x0.z = fmaf(-qv.z, c0v, x0.z); x0.w = fmaf(-qv.w, c0v, x0.w);
+      x1.x = fmaf(-qv.x, c1v, x1.x); x1.y = fmaf(-qv.y, c1v, x1.y);
+      x1.z = fmaf(-qv.z, c1v, x1.z); x1.w = fmaf(-qv.w, c1v, x1.w);
     }
-    __syncthreads();
-    for (int e = t; e < rows * w; e += THREADS) {
-      const int r = e % rows, jj = e / rows;
-      it.A[r0 + r + static_cast<int64_t>(c0 + jj) * it.lda] = s.a[jj * LD + r];
-    }
+    *reinterpret_cast<float4*>(&s.a[jj * LD + r]) = x0;
+    *reinterpret_cast<float4*>(&s.a[(jj + 1) * LD + r]) = x1;
   }
-  __syncthreads();
 }
 
-// G = A_p^T A_p (w x w, into s.g): warp wp takes rows 4 wp, 4 wp + 32, ... of
-// each chunk; lane (i = l / 4 .. ) owns 4 x 8 entries; warp partials are added
-// in warp order.
+// acc += the Gram matrix of a staged panel chunk (column-major at a): warp wp takes rows 4 wp,
+// 4 wp + 32, ...; lane (ti = l % 8, tj = l / 8) owns entries (ti + 8u, tj + 4v).
 template <int CR>
-__device__ void gram(Smem<CR>& s, const Item& it, int c0, int w) {
+__device__ __forceinline__ void chunk_gram(const float* a, int rq, float (&acc)[4][8]) {
   const int LD = CR + 4;
-  const int t = threadIdx.x;
-  const int lane = t % 32, wp = t / 32;
-  const int ti = lane % 8, tj = lane / 8;  // entries (ti + 8 u, tj + 4 v), u < 4, v < 8
-  float acc[4][8] = {};
-  for (int r0 = 0; r0 < it.m; r0 += CR) {
-    const int rows = min(CR, it.m - r0);
-    const int rq = (rows + 3) & ~3;
-    __syncthreads();
-    stage<CR>(s.a, it, r0, rows, c0, w);
-    __syncthreads();
-    for (int r = 4 * wp; r < rq; r += 32) {
-      float4 x[4], y[8];
+  const int lane = threadIdx.x % 32, wp = threadIdx.x / 32;
+  const int ti = lane % 8, tj = lane / 8;
+  for (int r = 4 * wp; r < rq; r += 32) {
+    float4 x[4], y[8];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) x[u] = *reinterpret_cast<const float4*>(&s.a[(ti + 8 * u) * LD + r]);
+    for (int u = 0; u < 4; ++u) x[u] = *reinterpret_cast<const float4*>(&a[(ti + 8 * u) * LD + r]);
 #pragma unroll
-      for (int v = 0; v < 8; ++v) y[v] = *reinterpret_cast<const float4*>(&s.a[(tj + 4 * v) * LD + r]);
+    for (int v = 0; v < 8; ++v) y[v] = *reinterpret_cast<const float4*>(&a[(tj + 4 * v) * LD + r]);
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 8; ++v)
-          acc[u][v] = fmaf(x[u].w, y[v].w, fmaf(x[u].z, y[v].z, fmaf(x[u].y, y[v].y, fmaf(x[u].x, y[v].x, acc[u][v]))));
-    }
+      for (int v = 0; v < 8; ++v)
+        acc[u][v] = fmaf(x[u].w, y[v].w, fmaf(x[u].z, y[v].z, fmaf(x[u].y, y[v].y, fmaf(x[u].x, y[v].x, acc[u][v]))));
   }
+}
+
+// G (w x w, into s.g) from the per-warp Gram accumulators, added in warp order.
+template <int CR>
+__device__ __forceinline__ void store_gram(Smem<CR>& s, int w, const float (&acc)[4][8]) {
+  const int lane = threadIdx.x % 32, wp = threadIdx.x / 32;
+  const int ti = lane % 8, tj = lane / 8;
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < 8; ++v) s.red[wp * PW * PW + (ti + 8 * u) * PW + tj + 4 * v] = acc[u][v];
   __syncthreads();
-  for (int e = t; e < PW * PW; e += THREADS) {
+  for (int e = threadIdx.x; e < PW * PW; e += THREADS) {
     float v = 0.f;
 #pragma unroll
     for (int q = 0; q < 8; ++q) v += s.red[q * PW * PW + e];
@@ -221,6 +196,67 @@ __device__ void gram(Smem<CR>& s, const Item& it, int c0, int w) {
     s.g[i][j] = (i < w && j < w) ? v : 0.f;
   }
   __syncthreads();
+}
+
+// M = L^-T (upper, into s.c as M[i][j] at i * (PW + 1) + j) for L = s.g (lower,
+// reciprocal diagonal in s.ginv), by warp 0: lane j solves L x = e_j by forward
+// substitution, x being column j of L^-1, i.e. row j of M.
+template <int CR>
+__device__ __forceinline__ void invert_factor(Smem<CR>& s, int w) {
+  if (threadIdx.x < 32) {
+    const int j = threadIdx.x;
+    float x[PW];
+#pragma unroll
+    for (int i = 0; i < PW; ++i) {
+      float v = (i == j) ? 1.f : 0.f;
+#pragma unroll
+      for (int k = 0; k < i; ++k) v = fmaf(-s.g[i][k], x[k], v);
+      x[i] = (i >= j && i < w) ? v * s.ginv[i] : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < PW; ++i) s.c[j * (PW + 1) + i] = x[i];
+  }
+  __syncthreads();
+}
+
+// out = in M (the staged chunk times the upper triangular M = L^-T, columns < w):
+// each thread computes a 4-row tile of the column pair (ct, PW - 1 - ct), so
+// every thread does the same number of multiply-adds.
+template <int CR>
+__device__ __forceinline__ void chunk_solve(const Smem<CR>& s, const float* in, float* out, int rq, int w) {
+  const int LD = CR + 4;
+  const int ntile = (rq / 4) * (PW / 2);
+  for (int e = threadIdx.x; e < ntile; e += THREADS) {
+    const int rt = e % (rq / 4), ct = e / (rq / 4);
+    const int r = 4 * rt, ja = ct, jb = PW - 1 - ct;
+    float4 xa = make_float4(0.f, 0.f, 0.f, 0.f), xb = xa;
+    const int ea = min(ja + 1, w), eb = min(jb + 1, w);
+    int i = 0;
+    for (; i < ea; ++i) {
+      const float4 v = *reinterpret_cast<const float4*>(&in[i * LD + r]);
+      const float ma = s.c[i * (PW + 1) + ja], mb = s.c[i * (PW + 1) + jb];
+      xa.x = fmaf(v.x, ma, xa.x); xa.y = fmaf(v.y, ma, xa.y); xa.z = fmaf(v.z, ma, xa.z); xa.w = fmaf(v.w, ma, xa.w);
+      xb.x = fmaf(v.x, mb, xb.x); xb.y = fmaf(v.y, mb, xb.y); xb.z = fmaf(v.z, mb, xb.z); xb.w = fmaf(v.w, mb, xb.w);
+    }
+    for (; i < eb; ++i) {
+      const float4 v = *reinterpret_cast<const float4*>(&in[i * LD + r]);
+      const float mb = s.c[i * (PW + 1) + jb];
+      xb.x = fmaf(v.x, mb, xb.x); xb.y = fmaf(v.y, mb, xb.y); xb.z = fmaf(v.z, mb, xb.z); xb.w = fmaf(v.w, mb, xb.w);
+    }
+    *reinterpret_cast<float4*>(&out[ja * LD + r]) = xa;
+    *reinterpret_cast<float4*>(&out[jb * LD + r]) = xb;
+  }
+}
+
+// A staged panel chunk (column-major at a) back to rows [r0, r0 + rows) of
+// columns [c0, c0 + w) of A.
+template <int CR>
+__device__ __forceinline__ void chunk_store(const float* a, const Item& it, int r0, int rows, int c0, int w) {
+  const int LD = CR + 4;
+  for (int e = threadIdx.x; e < rows * w; e += THREADS) {
+    const int r = e % rows, jj = e / rows;
+    it.A[r0 + r + static_cast<int64_t>(c0 + jj) * it.lda] = a[jj * LD + r];
+  }
 }
 
 // In-place lower Cholesky of s.g (w x w) by warp 0; returns false on a pivot <= 0.
@@ -254,29 +290,14 @@ __device__ bool chol(Smem<CR>& s, int w) {
   return bad == 0;
 }
 
-// A_p <- A_p L^-T (row-wise forward substitution), one thread per row.
-template <int CR>
-__device__ void trsm_rows(Smem<CR>& s, const Item& it, int c0, int w) {
-  for (int r = threadIdx.x; r < it.m; r += THREADS) {
-    float x[PW];
-#pragma unroll
-    for (int j = 0; j < PW; ++j) x[j] = j < w ? it.A[r + static_cast<int64_t>(c0 + j) * it.lda] : 0.f;
-#pragma unroll
-    for (int j = 0; j < PW; ++j) {
-      if (j < w) {
-        x[j] *= s.ginv[j];
-#pragma unroll
-        for (int i = j + 1; i < PW; ++i)
-          if (i < w) x[i] = fmaf(-x[j], s.g[i][j], x[i]);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < PW; ++j)
-      if (j < w) it.A[r + static_cast<int64_t>(c0 + j) * it.lda] = x[j];
-  }
-  __syncthreads();
-}
-
+// One matrix, panel by panel (left-looking), in five streams of row chunks per
+// panel, each fusing the products that share a staged chunk:
+//   1. C1 = Q^T A_p
+//   2. A_p -= Q C1, then C2 = Q^T A_p on the updated chunk
+//   3. A_p -= Q C2, then G1 = A_p^T A_p          (the first panel: G1 alone)
+//   4. A_p <- A_p L1^-T, then G2 = A_p^T A_p     (G1 = L1 L1^T)
+//   5. A_p <- A_p L2^-T                          (G2 = L2 L2^T)
+// R[<p, p] = C1 + C2, R[p, p] = L2^T L1^T.
 template <int CR>
 __global__ void __launch_bounds__(THREADS, 1) batched_qr_kernel(const Item* items, int count, int* queue, int* status) {
   extern __shared__ float smraw[];
@@ -296,30 +317,105 @@ __global__ void __launch_bounds__(THREADS, 1) batched_qr_kernel(const Item* item
       it.R[e % it.n + static_cast<int64_t>(e / it.n) * it.ldr] = 0.f;
     for (int c0 = 0; c0 < it.n; c0 += PW) {
       const int w = min(PW, it.n - c0);
-      // CGS2 against the previous panels.
-      if (c0 > 0) {
-        for (int pass = 0; pass < 2; ++pass) {
-          project(s, it, c0, w, c0);
-          for (int e = threadIdx.x; e < c0 * w; e += THREADS) {
-            const int i = e % c0, j = e / c0;
-            float* rp = &it.R[i + static_cast<int64_t>(c0 + j) * it.ldr];
-            *rp = (pass ? *rp : 0.f) + s.c[i * (PW + 1) + j];
-          }
-          subtract(s, it, c0, w, c0);
-        }
-      }
-      // CholQR2 inside the panel.
-      for (int pass = 0; pass < 2; ++pass) {
-        gram(s, it, c0, w);
-        ok &= chol(s, w);
-        trsm_rows(s, it, c0, w);
-        if (pass == 0) {
-          for (int e = threadIdx.x; e < PW * PW; e += THREADS) {
-            const int i = e % PW, j = e / PW;  // R1 = L1^T: R1[i][j] = L1[j][i], i <= j
-            r1[i][j] = (i <= j && j < w) ? s.g[j][i] : 0.f;
+      const int k1 = c0;  // previous Q columns
+      {
+        float gacc[4][8] = {};
+        if (k1 > 0) {
+          // Stream 1: C1.
+          float acc[(NMAX - PW) / 8] = {};
+          for (int r0 = 0; r0 < it.m; r0 += CR) {
+            const int rows = min(CR, it.m - r0), rq = (rows + 3) & ~3;
+            __syncthreads();
+            stage<CR>(s.q, it, r0, rows, 0, k1);
+            stage<CR>(s.a, it, r0, rows, c0, w);
+            __syncthreads();
+            chunk_project(s, rq, k1, acc);
           }
           __syncthreads();
+          store_projection(s, k1, w, acc);
+          __syncthreads();
+          for (int e = threadIdx.x; e < k1 * w; e += THREADS) {
+            const int i = e % k1, j = e / k1;
+            it.R[i + static_cast<int64_t>(c0 + j) * it.ldr] = s.c[i * (PW + 1) + j];
+          }
+          // Stream 2: A_p -= Q C1, C2 on the updated chunk.
+#pragma unroll
+          for (int u = 0; u < (NMAX - PW) / 8; ++u) acc[u] = 0.f;
+          for (int r0 = 0; r0 < it.m; r0 += CR) {
+            const int rows = min(CR, it.m - r0), rq = (rows + 3) & ~3;
+            __syncthreads();
+            stage<CR>(s.q, it, r0, rows, 0, k1);
+            stage<CR>(s.a, it, r0, rows, c0, w);
+            __syncthreads();
+            chunk_subtract(s, rq, k1);
+            __syncthreads();
+            chunk_project(s, rq, k1, acc);
+            chunk_store<CR>(s.a, it, r0, rows, c0, w);
+          }
+          __syncthreads();
+          store_projection(s, k1, w, acc);
+          __syncthreads();
+          for (int e = threadIdx.x; e < k1 * w; e += THREADS) {
+            const int i = e % k1, j = e / k1;
+            it.R[i + static_cast<int64_t>(c0 + j) * it.ldr] += s.c[i * (PW + 1) + j];
+          }
+          // Stream 3: A_p -= Q C2, G1.
+          for (int r0 = 0; r0 < it.m; r0 += CR) {
+            const int rows = min(CR, it.m - r0), rq = (rows + 3) & ~3;
+            __syncthreads();
+            stage<CR>(s.q, it, r0, rows, 0, k1);
+            stage<CR>(s.a, it, r0, rows, c0, w);
+            __syncthreads();
+            chunk_subtract(s, rq, k1);
+            __syncthreads();
+            chunk_gram<CR>(s.a, rq, gacc);
+            chunk_store<CR>(s.a, it, r0, rows, c0, w);
+          }
+        } else {
+          for (int r0 = 0; r0 < it.m; r0 += CR) {
+            const int rows = min(CR, it.m - r0), rq = (rows + 3) & ~3;
+            __syncthreads();
+            stage<CR>(s.a, it, r0, rows, c0, w);
+            __syncthreads();
+            chunk_gram<CR>(s.a, rq, gacc);
+          }
         }
+        __syncthreads();
+        store_gram(s, w, gacc);
+      }
+      ok &= chol(s, w);
+      invert_factor(s, w);
+      for (int e = threadIdx.x; e < PW * PW; e += THREADS) {
+        const int i = e % PW, j = e / PW;  // R1 = L1^T: R1[i][j] = L1[j][i], i <= j
+        r1[i][j] = (i <= j && j < w) ? s.g[j][i] : 0.f;
+      }
+      // Stream 4: A_p <- A_p L1^-T, G2 (the solved chunk goes to s.q, free here).
+      {
+        float gacc[4][8] = {};
+        for (int r0 = 0; r0 < it.m; r0 += CR) {
+          const int rows = min(CR, it.m - r0), rq = (rows + 3) & ~3;
+          __syncthreads();
+          stage<CR>(s.a, it, r0, rows, c0, w);
+          __syncthreads();
+          chunk_solve(s, s.a, s.q, rq, w);
+          __syncthreads();
+          chunk_gram<CR>(s.q, rq, gacc);
+          chunk_store<CR>(s.q, it, r0, rows, c0, w);
+        }
+        __syncthreads();
+        store_gram(s, w, gacc);
+      }
+      ok &= chol(s, w);
+      invert_factor(s, w);
+      // Stream 5: A_p <- A_p L2^-T.
+      for (int r0 = 0; r0 < it.m; r0 += CR) {
+        const int rows = min(CR, it.m - r0), rq = (rows + 3) & ~3;
+        __syncthreads();
+        stage<CR>(s.a, it, r0, rows, c0, w);
+        __syncthreads();
+        chunk_solve(s, s.a, s.q, rq, w);
+        __syncthreads();
+        chunk_store<CR>(s.q, it, r0, rows, c0, w);
       }
       // R[p,p] = L2^T R1 (upper x upper).
       for (int e = threadIdx.x; e < w * w; e += THREADS) {
