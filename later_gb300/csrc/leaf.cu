@@ -92,11 +92,17 @@ union LeafSmem {
   TsqrApplySmem ta;
 };
 
-__device__ __forceinline__ int ld_acquire(const int* p) {
+__device__ __forceinline__ int ld_relaxed(const int* p) {
   int v;
-  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+
+__device__ __forceinline__ void red_release_add(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
 // Grid-wide barrier over the co-resident CTAs of a cooperative launch.
 // Monotonic arrival counter; every wait is bounded: on timeout the status word
@@ -113,25 +119,29 @@ __device__ bool grid_barrier(GridSync& g, int* okflag) {
   __syncthreads();
   ++g.epoch;
   if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(g.arrive, 1);
+    // Arrive with release semantics (the CTA's writes, ordered before it by
+    // __syncthreads, become visible first); poll with relaxed loads, one L2
+    // round trip per poll, the abort flag and the clock every eighth poll;
+    // then one acquire fence.
+    red_release_add(g.arrive, 1);
     const int target = g.epoch * static_cast<int>(gridDim.x);
     const long long t0 = clock64();
     int good = 1;
-    while (ld_acquire(g.arrive) < target) {
-      if (ld_acquire(g.abort)) {
-        good = 0;
-        break;
+    for (unsigned it = 1; ld_relaxed(g.arrive) < target; ++it) {
+      if ((it & 7) == 0) {
+        if (ld_relaxed(g.abort)) {
+          good = 0;
+          break;
+        }
+        if (clock64() - t0 > g.budget) {
+          report(g.status, DEV_TIMEOUT);
+          atomicExch(g.abort, 1);
+          good = 0;
+          break;
+        }
       }
-      if (clock64() - t0 > g.budget) {
-        report(g.status, DEV_TIMEOUT);
-        atomicExch(g.abort, 1);
-        good = 0;
-        break;
-      }
-      __nanosleep(64);
     }
-    __threadfence();
+    fence_acq_rel();
     *okflag = good;
   }
   __syncthreads();
