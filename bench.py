@@ -1,10 +1,13 @@
 """Benchmark: recursive tensor-core QR (later_rgsqrf) on one GB300.
 
 Workload (default): rgsqrf of a 16384 x 16384 FP32 matrix, entries N(0,1)
-from a fixed seed, FP16 tensor-core trailing updates with FP32 accumulation,
-leaf panel width 128 — the square shape of the QR precision sweep. The metric
-is the reference's QR rate, 2 n^2 (m - n/3) / t (test/test_qr.cu:85-86), in
-TFLOP/s, reported beside the backward error ||A - QR|| / ||A||.
+from a fixed seed, leaf panel width 128 — the square shape of the QR precision
+sweep — with SPLIT2 tensor-core trailing updates (FP16 products, FP32
+accumulation, the update's Q operand split hi + lo), the mode whose backward
+error ||A - QR|| / ||A|| stays below 1e-5. The same matrix is also timed with
+plain FP16 updates (the reference's only mode) and reported under
+`alt_precision`. The metric is the reference's QR rate, 2 n^2 (m - n/3) / t
+(test/test_qr.cu:85-86), in TFLOP/s, reported beside the backward error.
 
 A step is one QR of the full matrix. The matrix (1 GiB) is larger than L2, and
 it is restored from a pristine device copy before each step (outside the
@@ -49,7 +52,10 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--m", type=int, default=16384)
     p.add_argument("--n", type=int, default=16384)
-    p.add_argument("--precision", default="fp16", choices=["fp16", "bf16", "split3"])
+    p.add_argument("--precision", default=None, choices=["fp16", "bf16", "split3", "split2"],
+                   help="tensor-core precision (default: split2 for qr, fp16 for spd)")
+    p.add_argument("--alt-precision", default="fp16", choices=["none", "fp16", "bf16", "split3", "split2"],
+                   help="qr: also time this precision on the same matrix (reported under alt_precision)")
     p.add_argument("--leaf", type=int, default=128)
     p.add_argument("--panel", default="fused", choices=["fused", "wide", "mgs"],
                    help="rgsqrf leaf: fused 32-column CholQR2 panels (default), fused leaf-wide CholQR2 first, "
@@ -130,15 +136,16 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baselines
-def cpu_oracle_rate(m, n, seed, threads=None):
-    """Times the oracle restatement of later_rgsqrf (numpy, all host threads) on an m x n sample."""
+def cpu_oracle_rate(m, n, seed, prec="fp16"):
+    """Times the oracle restatement of later_rgsqrf (numpy, all host threads) on an m x n sample;
+    prec fp16 is the reference's own arithmetic."""
     import numpy as np
     from oracle import gen
     from oracle import later_oracle as lo
     A = gen.normal(m, n, seed)
-    lo.rgsqrf(A[: min(m, 2048), : min(n, 256)])  # warm-up (BLAS threads, caches)
+    lo.rgsqrf(A[: min(m, 2048), : min(n, 256)], prec=prec)  # warm-up (BLAS threads, caches)
     t = time.perf_counter()
-    lo.rgsqrf(A)
+    lo.rgsqrf(A, prec=prec)
     dt = time.perf_counter() - t
     return qr_flops(m, n) / dt / 1e12, dt
 
@@ -169,7 +176,8 @@ def run_reference(a, rank, world):
         r, _ = cpu_oracle_rate(a.cpu_m, a.cpu_n, a.seed)
         rates.append(r)
     v = statistics.median(rates)
-    sample = f"oracle restatement of later_rgsqrf (numpy, fp16-rounded GEMM operands) on {a.cpu_m}x{a.cpu_n}, N(0,1) seed {a.seed}"
+    sample = (f"oracle restatement of later_rgsqrf in the reference's own FP16 arithmetic (numpy, fp16-rounded "
+              f"GEMM operands) on {a.cpu_m}x{a.cpu_n}, N(0,1) seed {a.seed}")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": qr_flops(a.cpu_m, a.cpu_n) / v / 1e9,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": a.precision,
@@ -248,6 +256,36 @@ def run_ours(a, rank, world, local_rank):
     orth = (eye - A.t() @ A).norm()
     bwd, orth = float(res), float(orth)
 
+    # ---- the same matrix in a second precision (the reference's FP16 by default)
+    alt = None
+    if a.alt_precision not in ("none", a.precision):
+        lw2, lh2 = lg.rgsqrf_bufsize(m, n, a.alt_precision, a.cgs2, a.leaf)
+        work2 = work if lw2 <= lw else torch.empty(lw2, dtype=torch.float32, device=dev)
+        hwork2 = hwork if lh2 <= lh else torch.empty(lh2, dtype=torch.float16, device=dev)
+
+        def qr_alt():
+            lg.later_rgsqrf(A, R, work2, hwork2, precision=a.alt_precision, cgs2=a.cgs2, leaf=a.leaf,
+                            panel=a.panel)
+
+        for _ in range(2):
+            A.copy_(A0)
+            qr_alt()
+        ms_alt = []
+        for _ in range(a.steps):
+            A.copy_(A0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            qr_alt()
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms_alt.append(e0.elapsed_time(e1))
+        bwd_alt = float((A0 - A @ torch.triu(R)).norm() / A0.norm())
+        orth_alt = float((eye - A.t() @ A).norm())
+        ma = sum(ms_alt) / len(ms_alt)
+        alt = {a.alt_precision: {"value": flops / ma / 1e9, "unit": "TFLOP/s", "ms_per_step": ma,
+                                 "steps": a.steps, "backward_error": bwd_alt, "orthogonality_over_n": orth_alt / n}}
+
     # ---- per-class trace of one extra step (roofline of the dominant kernel)
     A.copy_(A0)
     lg.trace_begin()
@@ -315,7 +353,7 @@ def run_ours(a, rank, world, local_rank):
     hbm_src = "measured copy bandwidth (MEASURED_PEAKS.json)" if hbm else "fallback 6800 GB/s"
     hbm = hbm or 6800.0
     w = min(n, a.leaf)
-    leaf_bytes = m * w * (4 + 4 + (4 if a.precision == "split3" else 2))
+    leaf_bytes = m * w * (4 + 4 + (4 if a.precision in ("split3", "split2") else 2))
     leaf_ms = tr["panel_ms"] / tr["panel_launches"] if tr["panel_launches"] else None
     leaf_ach = leaf_bytes / leaf_ms / 1e6 if leaf_ms else None
     leaf_traffic = None
@@ -346,7 +384,7 @@ def run_ours(a, rank, world, local_rank):
             "config": workload_config(a),
             "accuracy": {"backward_error": bwd, "orthogonality_fro": orth, "orthogonality_over_n": orth / n,
                          "computed": "FP32 on GPU, TF32 off (as test/test_qr.cu:216-268)"},
-            "executed_tflops": 2.0 * m * n * n / ms_step / 1e9,
+            "executed_tflops": 2.0 * m * n * n / ms_step / 1e9, "alt_precision": alt,
             "roofline": roof, "roofline_gemm": roof_gemm, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "launches_per_step": launches / max(1, a.steps), "clocks": clocks,
             "wall_s_timed_region": t_wall,
@@ -599,6 +637,8 @@ def run_serve(a):
 
 def main():
     a = parse()
+    if a.precision is None:
+        a.precision = "split2" if a.config == "qr" else "fp16"
     if a.gemm:
         run_gemm_only(a)
         return

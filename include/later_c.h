@@ -39,7 +39,10 @@ typedef enum {
 typedef enum {
   LATER_PREC_FP16 = 0,  /* FP16 tensor-core products, FP32 accumulation (reference behaviour) */
   LATER_PREC_BF16 = 1,  /* BF16 products, FP32 accumulation (range-safe) */
-  LATER_PREC_SPLIT3 = 2 /* hi+lo FP16 split, three products per GEMM: ~FP32 accuracy */
+  LATER_PREC_SPLIT3 = 2, /* hi+lo FP16 split, three products per GEMM: ~FP32 accuracy */
+  LATER_PREC_SPLIT2 = 3  /* rgsqrf (and the LS solver) only: R12 = Q1^T A2 as one FP16 product kept at its
+                            FP16 value, A2 -= Q1 R12 with Q1 split hi+lo (two products): backward error at
+                            the FP32 level, orthogonality as FP16, 1.5x the FP16 tensor work */
 } later_precision_t;
 
 typedef struct {

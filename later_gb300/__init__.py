@@ -25,7 +25,7 @@ __all__ = [
     "trace_end",
 ]
 
-PREC = {"fp16": 0, "bf16": 1, "split3": 2}
+PREC = {"fp16": 0, "bf16": 1, "split3": 2, "split2": 3}
 STATUS = {0: "ok", 1: "invalid argument", 2: "workspace too small", 3: "CUDA runtime error",
           4: "device wait timed out", 5: "not supported", 6: "value outside the FP16 operand range",
           7: "non-positive pivot"}

@@ -52,11 +52,6 @@ __device__ __forceinline__ void put16(void* hi, void* lo, int64_t o, float v, in
   }
 }
 
-// Zeros `n` floats of shared memory (16-byte aligned, n a multiple of 4).
-__device__ __forceinline__ void zero_smem(float* p, int n) {
-  for (int e = threadIdx.x; e < n / 4; e += blockDim.x) reinterpret_cast<float4*>(p)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-}
-
 // Copies the nb x nb lower triangle of column-major L (ld ldl) into shared
 // memory, element (i, j) at dst[i * si + j * sj]; zeros above the diagonal.
 // Global reads are coalesced (i fastest) and issued eight per thread before
@@ -716,6 +711,7 @@ int64_t splitk_work() { return static_cast<int64_t>(num_sms()) * 128 * 256 * 2 +
 
 later_status_t rsyrk(cudaStream_t st, int n, int k, float alpha, const float* A, int64_t lda, float beta, float* C,
                      int64_t ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
+  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;  // SPLIT2 is rgsqrf's
   if (n < 0 || k < 0 || lda < std::max(n, 1) || ldc < std::max(n, 1) || !A || !C) return LATER_ERR_INVALID_ARG;
   if (n == 0) return LATER_OK;
   if (!hwork || lhwork < rsyrk_hwork(n, k, o) || (reinterpret_cast<uintptr_t>(hwork) & 15)) return LATER_ERR_WORKSPACE;
@@ -736,6 +732,7 @@ later_status_t rtrsm(cudaStream_t st, char uplo, char leri, char trans, int m, i
 later_status_t rtrsm_lim(cudaStream_t st, char uplo, char leri, char trans, int m, int n, const float* A,
                          int64_t lda, float* B, int64_t ldb, float* work, int64_t lwork, void* hwork, int64_t lhwork,
                          const Options& o, int fp32_lim) {
+  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;  // SPLIT2 is rgsqrf's
   auto lc = [](char c) { return static_cast<char>(c | 0x20); };
   const char u = lc(uplo), s = lc(leri), t = lc(trans);
   const bool lln = (u == 'l' && s == 'l' && t == 'n');
@@ -766,6 +763,7 @@ later_status_t rtrsm_lim(cudaStream_t st, char uplo, char leri, char trans, int 
 later_status_t rtrmm(cudaStream_t st, int m, int n, const float* A, int64_t lda, const float* B, int64_t ldb,
                      float* C, int64_t ldc, float* work, int64_t lwork, void* hwork, int64_t lhwork,
                      const Options& o) {
+  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;  // SPLIT2 is rgsqrf's
   if (m < 0 || n < 0 || !A || !B || !C || lda < std::max(m, 1) || ldb < std::max(m, 1) || ldc < std::max(m, 1))
     return LATER_ERR_INVALID_ARG;
   if (m == 0 || n == 0) return LATER_OK;
@@ -781,6 +779,7 @@ later_status_t rtrmm(cudaStream_t st, int m, int n, const float* A, int64_t lda,
 
 later_status_t rpotrf(cudaStream_t st, char uplo, int n, float* A, int64_t lda, float* work, int64_t lwork,
                       void* hwork, int64_t lhwork, const Options& o) {
+  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;  // SPLIT2 is rgsqrf's
   if ((uplo | 0x20) != 'l') return LATER_ERR_NOT_SUPPORTED;
   if (n < 0 || !A || lda < std::max(n, 1)) return LATER_ERR_INVALID_ARG;
   if (n == 0) return LATER_OK;

@@ -86,7 +86,7 @@ later_status_t later_c_ormqr(later_stream_t stream, int m, int n, float* W, int 
 later_status_t later_c_blas3_bufsize(char op, char side, int m, int n, const later_options_t* opt, int64_t* lwork,
                                      int64_t* lhwork) {
   const Options o = options_from(opt);
-  if (m < 0 || n < 0) return LATER_ERR_INVALID_ARG;
+  if (m < 0 || n < 0 || o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;
   int64_t h = 0;
   switch (op | 0x20) {
     case 's': h = rsyrk_hwork(m, n, o); break;

@@ -55,6 +55,7 @@ struct GemmArgs {
   int out_mode;  // 0 fp16, 1 bf16, 2 split3 (hi/lo fp16)
   int lower, diag;
   int shadow_acc;
+  int round_prod;
   int ab_bf16;
   float* partial;
   int* counters;
@@ -74,7 +75,8 @@ __device__ __forceinline__ void store16(void* base, int64_t idx, float v, int bf
 __device__ __forceinline__ void epilogue_store_c(const GemmArgs& p, int row, int col, float acc, float c) {
   if (row >= p.M || col >= p.N) return;
   if (p.lower && row < col + p.diag) return;
-  const float prod = p.alpha * acc;
+  float prod = p.alpha * acc;
+  if (p.round_prod) prod = __half2float(__float2half_rn(prod));
   float v = prod;
   if (p.beta != 0.f) v += p.beta * c;
   p.D[row + static_cast<int64_t>(col) * p.ldd] = v;
@@ -93,22 +95,25 @@ __device__ __forceinline__ void epilogue_store_c(const GemmArgs& p, int row, int
   }
 }
 
-template <int BN, bool A_MN, bool B_MN, bool SPLIT, int STAGES>
+// SPL: 0 one product; 1 A split (hi.hi into accumulator 0, lo.hi into 1);
+// 2 both split, SPLIT3 (hi.hi into 0, hi.lo + lo.hi into 1).
+template <int BN, bool A_MN, bool B_MN, int SPL, int STAGES>
 struct Cfg {
   static constexpr int A_BYTES = BM * BK * 2;  // 16 KB
   static constexpr int B_BYTES = BN * BK * 2;
-  static constexpr int NOPS = SPLIT ? 2 : 1;
-  static constexpr int STAGE_BYTES = NOPS * (A_BYTES + B_BYTES);
-  static constexpr int TMEM_COLS = SPLIT ? 2 * BN : BN;
+  static constexpr int A_OPS = SPL ? 2 : 1;
+  static constexpr int B_OPS = SPL == 2 ? 2 : 1;
+  static constexpr int STAGE_BYTES = A_OPS * A_BYTES + B_OPS * B_BYTES;
+  static constexpr int TMEM_COLS = SPL ? 2 * BN : BN;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 };
 
-template <int BN, bool A_MN, bool B_MN, bool SPLIT, int STAGES>
+template <int BN, bool A_MN, bool B_MN, int SPL, int STAGES>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const __grid_constant__ CUtensorMap tmAl, const __grid_constant__ CUtensorMap tmBl,
                    const GemmArgs p) {
-  using C_ = Cfg<BN, A_MN, B_MN, SPLIT, STAGES>;
+  using C_ = Cfg<BN, A_MN, B_MN, SPL, STAGES>;
   static_assert(C_::TMEM_COLS >= 32 && C_::TMEM_COLS <= 512, "tmem");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -153,10 +158,8 @@ __global__ void __launch_bounds__(128, 1)
       // ------------------------------------------------------- producer
       tma_prefetch_desc(&tmA);
       tma_prefetch_desc(&tmB);
-      if (SPLIT) {
-        tma_prefetch_desc(&tmAl);
-        tma_prefetch_desc(&tmBl);
-      }
+      if (SPL) tma_prefetch_desc(&tmAl);
+      if (SPL == 2) tma_prefetch_desc(&tmBl);
       int issued = 0;
       for (int i = 0; i < nkb; ++i) {
         const int s = i % STAGES;
@@ -167,21 +170,24 @@ __global__ void __launch_bounds__(128, 1)
         }
         if (*abort_flag) break;
         uint8_t* sa = smem + s * C_::STAGE_BYTES;
-        uint8_t* sb = sa + C_::NOPS * C_::A_BYTES;
+        uint8_t* sb = sa + C_::A_OPS * C_::A_BYTES;
         const int k0 = (kb0 + i) * BK;
         mbar_arrive_expect_tx(&full[s], C_::STAGE_BYTES);
 #pragma unroll
-        for (int op = 0; op < C_::NOPS; ++op) {
+        for (int op = 0; op < C_::A_OPS; ++op) {
           const CUtensorMap* ma = op ? &tmAl : &tmA;
-          const CUtensorMap* mb = op ? &tmBl : &tmB;
           uint8_t* da = sa + op * C_::A_BYTES;
-          uint8_t* db = sb + op * C_::B_BYTES;
           if (A_MN) {
             tma_load_2d(da, ma, &full[s], m0, k0);
             tma_load_2d(da + BK * 128, ma, &full[s], m0 + 64, k0);
           } else {
             tma_load_2d(da, ma, &full[s], k0, m0);
           }
+        }
+#pragma unroll
+        for (int op = 0; op < C_::B_OPS; ++op) {
+          const CUtensorMap* mb = op ? &tmBl : &tmB;
+          uint8_t* db = sb + op * C_::B_BYTES;
           if (B_MN) {
 #pragma unroll
             for (int c = 0; c < BN / 64; ++c) tma_load_2d(db + c * BK * 128, mb, &full[s], n0 + 64 * c, k0);
@@ -209,7 +215,7 @@ __global__ void __launch_bounds__(128, 1)
         if (*abort_flag) break;
         tc_fence_after();
         const uint32_t sa = smem_u32(smem + s * C_::STAGE_BYTES);
-        const uint32_t sb = sa + C_::NOPS * C_::A_BYTES;
+        const uint32_t sb = sa + C_::A_OPS * C_::A_BYTES;
 #pragma unroll
         for (int k = 0; k < BK / 16; ++k) {
           // A: K-major -> advance 32 B within the swizzled row; MN-major -> 16 K-rows.
@@ -219,11 +225,14 @@ __global__ void __launch_bounds__(128, 1)
           const uint64_t bd = smem_desc_sw128(sb + b_off, B_MN ? BK * 128 : 16, 1024);
           const uint32_t acc = (i > 0 || k > 0) ? 1u : 0u;
           tc_mma_f16(tmem, ad, bd, idesc, acc);
-          if (SPLIT) {
+          if (SPL == 2) {
             const uint64_t adl = smem_desc_sw128(sa + C_::A_BYTES + a_off, A_MN ? BK * 128 : 16, 1024);
             const uint64_t bdl = smem_desc_sw128(sb + C_::B_BYTES + b_off, B_MN ? BK * 128 : 16, 1024);
             tc_mma_f16(tmem + BN, ad, bdl, idesc, acc);
             tc_mma_f16(tmem + BN, adl, bd, idesc, 1u);
+          } else if (SPL == 1) {
+            const uint64_t adl = smem_desc_sw128(sa + C_::A_BYTES + a_off, A_MN ? BK * 128 : 16, 1024);
+            tc_mma_f16(tmem + BN, adl, bd, idesc, acc);
           }
         }
         tc_commit(&empty[s]);
@@ -249,7 +258,7 @@ __global__ void __launch_bounds__(128, 1)
   for (int c0 = 0; c0 < BN; c0 += 32) {
     float v[32];
     tmem_ld_32x32b_x32(t_row + c0, v);
-    if (SPLIT) {
+    if (SPL) {
       float w[32];
       tmem_ld_32x32b_x32(t_row + BN + c0, w);
 #pragma unroll
@@ -328,11 +337,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-template <int BN, bool A_MN, bool B_MN, bool SPLIT, int STAGES>
+template <int BN, bool A_MN, bool B_MN, int SPL, int STAGES>
 later_status_t launch_cfg(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& al,
                           const CUtensorMap& bl, const GemmArgs& args, dim3 grid, cudaStream_t st) {
-  using C_ = Cfg<BN, A_MN, B_MN, SPLIT, STAGES>;
-  auto kern = tc_gemm_kernel<BN, A_MN, B_MN, SPLIT, STAGES>;
+  using C_ = Cfg<BN, A_MN, B_MN, SPL, STAGES>;
+  static_assert(C_::SMEM <= 227 * 1024, "shared memory");
+  auto kern = tc_gemm_kernel<BN, A_MN, B_MN, SPL, STAGES>;
   static bool attr_done[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -352,14 +362,14 @@ later_status_t launch_cfg(const CUtensorMap& a, const CUtensorMap& b, const CUte
   return LATER_OK;
 }
 
-template <int BN, bool SPLIT, int STAGES>
+template <int BN, int SPL, int STAGES>
 later_status_t launch_bn(bool a_mn, bool b_mn, const CUtensorMap& a, const CUtensorMap& b,
                          const CUtensorMap& al, const CUtensorMap& bl, const GemmArgs& args, dim3 grid,
                          cudaStream_t st) {
-  if (!a_mn && !b_mn) return launch_cfg<BN, false, false, SPLIT, STAGES>(a, b, al, bl, args, grid, st);
-  if (a_mn && !b_mn) return launch_cfg<BN, true, false, SPLIT, STAGES>(a, b, al, bl, args, grid, st);
-  if (a_mn && b_mn) return launch_cfg<BN, true, true, SPLIT, STAGES>(a, b, al, bl, args, grid, st);
-  return launch_cfg<BN, false, true, SPLIT, STAGES>(a, b, al, bl, args, grid, st);
+  if (!a_mn && !b_mn) return launch_cfg<BN, false, false, SPL, STAGES>(a, b, al, bl, args, grid, st);
+  if (a_mn && !b_mn) return launch_cfg<BN, true, false, SPL, STAGES>(a, b, al, bl, args, grid, st);
+  if (a_mn && b_mn) return launch_cfg<BN, true, true, SPL, STAGES>(a, b, al, bl, args, grid, st);
+  return launch_cfg<BN, false, true, SPL, STAGES>(a, b, al, bl, args, grid, st);
 }
 
 }  // namespace
@@ -386,8 +396,11 @@ later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, lon
   const bool a_mn = (g.ta == 'N' || g.ta == 'n');
   const bool b_mn = (g.tb == 'T' || g.tb == 't');
   const bool split3 = (g.prec == LATER_PREC_SPLIT3);
+  const bool split_a = (g.prec == LATER_PREC_SPLIT2);  // A = hi + lo, B = hi: two products
   const bool bf16 = (g.prec == LATER_PREC_BF16);
+  if (g.prec < LATER_PREC_FP16 || g.prec > LATER_PREC_SPLIT2) return LATER_ERR_INVALID_ARG;
   if (split3 && (!g.A.lo || !g.B.lo)) return LATER_ERR_INVALID_ARG;
+  if (split_a && (!g.A.lo || !a_mn || b_mn)) return LATER_ERR_INVALID_ARG;  // the A2 -= Q1 R12 shape only
   if (g.out.Dh && g.out_prec == LATER_PREC_SPLIT3 && !g.out.Dl) return LATER_ERR_INVALID_ARG;
 
   // Tile width: the widest of 256 / 128 / 64 that still gives the GPU enough tiles.
@@ -431,10 +444,11 @@ later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, lon
   a.Dh = g.out.Dh;
   a.Dl = g.out.Dl;
   a.ldh = g.out.ldh;
-  a.out_mode = g.out_prec == LATER_PREC_BF16 ? 1 : (g.out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
+  a.out_mode = g.out_prec == LATER_PREC_BF16 ? 1 : (g.out_prec == LATER_PREC_SPLIT3 ? 2 : 0);  // SPLIT2: hi only
   a.lower = g.out.lower;
   a.diag = g.out.diag;
   a.shadow_acc = g.out.shadow_acc;
+  a.round_prod = g.out.round_prod;
   a.ab_bf16 = bf16 ? 1 : 0;
   a.partial = s.partial;
   a.counters = s.counters;
@@ -449,23 +463,29 @@ later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, lon
   const uint32_t b_box_c = b_mn ? BK : BN;
   if (!make_map16(&ma, g.A.hi, a_rows, a_cols, g.A.ld, 64, a_box_c, bf16)) return LATER_ERR_INVALID_ARG;
   if (!make_map16(&mb, g.B.hi, b_rows, b_cols, g.B.ld, 64, b_box_c, bf16)) return LATER_ERR_INVALID_ARG;
-  if (split3) {
+  mal = ma;
+  mbl = mb;
+  if (split3 || split_a) {
     if (!make_map16(&mal, g.A.lo, a_rows, a_cols, g.A.ld, 64, a_box_c, false)) return LATER_ERR_INVALID_ARG;
+  }
+  if (split3) {
     if (!make_map16(&mbl, g.B.lo, b_rows, b_cols, g.B.ld, 64, b_box_c, false)) return LATER_ERR_INVALID_ARG;
-  } else {
-    mal = ma;
-    mbl = mb;
   }
 
   dim3 grid(tiles, splits);
   TraceScope trace(st, TRACE_GEMM, 2.0 * g.M * g.N * static_cast<double>(g.K));
   if (split3) {
-    if (BN == 64) return launch_bn<64, true, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
-    return launch_bn<128, true, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+    if (BN == 64) return launch_bn<64, 2, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+    return launch_bn<128, 2, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
   }
-  if (BN == 64) return launch_bn<64, false, 6>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
-  if (BN == 128) return launch_bn<128, false, 4>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
-  return launch_bn<256, false, 4>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+  if (split_a) {  // A MN-major, B K-major (checked above)
+    if (BN == 64) return launch_cfg<64, true, false, 1, 4>(ma, mb, mal, mbl, a, grid, st);
+    if (BN == 128) return launch_cfg<128, true, false, 1, 4>(ma, mb, mal, mbl, a, grid, st);
+    return launch_cfg<256, true, false, 1, 3>(ma, mb, mal, mbl, a, grid, st);
+  }
+  if (BN == 64) return launch_bn<64, 0, 6>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+  if (BN == 128) return launch_bn<128, 0, 4>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
+  return launch_bn<256, 0, 4>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
 }
 
 }  // namespace later

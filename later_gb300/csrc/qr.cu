@@ -55,6 +55,12 @@ struct Ctx {
 
 inline char* col16(char* base, int64_t ld, int64_t j) { return base ? base + j * ld * 2 : nullptr; }
 
+// Format of the 16-bit copy of Q the panels write: SPLIT2 needs Q's lo part
+// (the A operand of A2 -= Q1 R12), so its panels write hi and lo as SPLIT3 does.
+inline int panel_out_prec(int prec) { return prec == LATER_PREC_SPLIT2 ? LATER_PREC_SPLIT3 : prec; }
+// Operand format of R12 = Q1^T A2 (SPLIT2: one FP16 product).
+inline int proj_prec(int prec) { return prec == LATER_PREC_SPLIT2 ? LATER_PREC_FP16 : prec; }
+
 Scratch gemm_scratch(Ctx& c) {
   Scratch s;
   s.counters = c.counters + 2048;
@@ -73,7 +79,7 @@ Scratch gemm_scratch(Ctx& c) {
 later_status_t leaf_qr(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
   if (w <= 32) {
     return tsqr_panel(c.st, c.m, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
-                      c.o.prec, *c.ws, c.counters, c.o.budget, w);
+                      panel_out_prec(c.o.prec), *c.ws, c.counters, c.o.budget, w);
   }
   const int w1 = split_half(w), w2 = w - w1;
   LATER_CHECK(leaf_qr(c, w1, A, lda, R, ldr, col));
@@ -95,7 +101,8 @@ later_status_t leaf_top(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t 
   if ((c.o.panel == 0 || c.o.panel == 2) && w <= kLeafMaxWidth) {
     const later_status_t s =
         leaf_fused(c.st, c.m, w, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
-                   c.o.prec, c.o.cgs2, c.o.panel == 2, *c.ws, c.counters + 4096, c.counters, c.o.budget, nullptr);
+                   panel_out_prec(c.o.prec), c.o.cgs2, c.o.panel == 2, *c.ws, c.counters + 4096, c.counters,
+                   c.o.budget, nullptr);
     if (s != LATER_ERR_NOT_SUPPORTED && s != LATER_ERR_WORKSPACE) return s;
   }
   return leaf_qr(c, w, A, lda, R, ldr, col);
@@ -112,7 +119,9 @@ later_status_t rec_qr(Ctx& c, int n, float* A, int64_t lda, float* R, int64_t ld
   Op16 R12h{c.r12h, c.r12l, c.ldr12};
   const int passes = c.o.cgs2 ? 2 : 1;
   for (int pass = 0; pass < passes; ++pass) {
-    // R12 (+)= Q1^T A2, FP32 into R, 16-bit copy of this pass's product.
+    // R12 (+)= Q1^T A2, FP32 into R, 16-bit copy of this pass's product. In
+    // SPLIT2 the product is one FP16 GEMM and R keeps its FP16-rounded value,
+    // the exact factor the update below subtracts.
     GemmCall tn;
     tn.ta = 'T';
     tn.tb = 'N';
@@ -131,10 +140,12 @@ later_status_t rec_qr(Ctx& c, int n, float* A, int64_t lda, float* R, int64_t ld
     tn.out.Dl = c.r12l;
     tn.out.ldh = c.ldr12;
     tn.out.shadow_acc = 1;
-    tn.prec = c.o.prec;
-    tn.out_prec = c.o.prec;
+    tn.out.round_prod = c.o.prec == LATER_PREC_SPLIT2 ? 1 : 0;
+    tn.prec = proj_prec(c.o.prec);
+    tn.out_prec = proj_prec(c.o.prec);
     LATER_CHECK(tc_gemm(tn, gemm_scratch(c), c.st, c.o.budget));
-    // A2 -= Q1 R12 in FP32, refreshing A2's 16-bit copy.
+    // A2 -= Q1 R12 in FP32, refreshing A2's 16-bit copy (SPLIT2: Q1 = hi + lo,
+    // R12 FP16; A2's copy hi only, its lo is written by A2's own panels).
     GemmCall nn;
     nn.ta = 'N';
     nn.tb = 'N';
@@ -153,7 +164,7 @@ later_status_t rec_qr(Ctx& c, int n, float* A, int64_t lda, float* R, int64_t ld
     nn.out.Dl = const_cast<void*>(A2h.lo);
     nn.out.ldh = c.ldh;
     nn.prec = c.o.prec;
-    nn.out_prec = c.o.prec;
+    nn.out_prec = proj_prec(c.o.prec);
     LATER_CHECK(tc_gemm(nn, gemm_scratch(c), c.st, c.o.budget));
   }
   return rec_qr(c, n2, A2, lda, R + n1 + n1 * ldr, ldr, col + n1);
@@ -209,7 +220,7 @@ QrNeed rgsqrf_need(int m, int n, const Options& o) {
   q.min_work = fixed + std::max<int64_t>(stack, 4096 + 128);
   q.rec_work = fixed + std::max(std::max(std::max(stack, leaf_parts), splitk), leaf_fused_work(m));
   const int64_t ldh = round_up(m, 8);
-  q.hwork = ldh * n * (o.prec == LATER_PREC_SPLIT3 ? 2 : 1);
+  q.hwork = ldh * n * (o.prec == LATER_PREC_SPLIT3 || o.prec == LATER_PREC_SPLIT2 ? 2 : 1);
   return q;
 }
 
@@ -217,7 +228,7 @@ later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, floa
                       int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
   if (m < 1 || n < 1 || m < n || lda < m || ldr < n || !A || !R) return LATER_ERR_INVALID_ARG;
   if (o.leaf != 32 && o.leaf != 64 && o.leaf != 128) return LATER_ERR_INVALID_ARG;
-  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;
+  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT2) return LATER_ERR_INVALID_ARG;
   const QrNeed need = rgsqrf_need(m, n, o);
   if (!work || !hwork || lwork < need.min_work || lhwork < need.hwork) return LATER_ERR_WORKSPACE;
   if ((reinterpret_cast<uintptr_t>(hwork) & 15) != 0) return LATER_ERR_INVALID_ARG;
@@ -233,7 +244,7 @@ later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, floa
   c.counters = L.counters;
   c.ldh = round_up(m, 8);
   c.sh_hi = static_cast<char*>(hwork);
-  c.sh_lo = o.prec == LATER_PREC_SPLIT3 ? c.sh_hi + c.ldh * n * 2 : nullptr;
+  c.sh_lo = (o.prec == LATER_PREC_SPLIT3 || o.prec == LATER_PREC_SPLIT2) ? c.sh_hi + c.ldh * n * 2 : nullptr;
   c.r12h = L.r12h;
   c.r12l = L.r12l;
   c.ldr12 = L.ldr12;
@@ -243,8 +254,10 @@ later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, floa
   LATER_CHECK_CUDA(cudaMemsetAsync(L.counters, 0, kCounters * sizeof(int), st));
   LATER_CHECK(fill_strict_lower(st, n, n, R, ldr, 0.f));
   const int f = first_leaf(n, o.leaf);
+  // The columns' 16-bit copy as the projections read it (SPLIT2: hi only).
   LATER_CHECK(convert16(st, m, n - f, A + static_cast<int64_t>(f) * lda, lda, c.sh_hi + f * c.ldh * 2,
-                        c.sh_lo ? c.sh_lo + f * c.ldh * 2 : nullptr, c.ldh, o.prec));
+                        (c.sh_lo && o.prec == LATER_PREC_SPLIT3) ? c.sh_lo + f * c.ldh * 2 : nullptr, c.ldh,
+                        proj_prec(o.prec)));
   return rec_qr(c, n, A, lda, R, ldr, 0);
 }
 

@@ -67,6 +67,7 @@ struct GemmOut {
   int lower = 0;             // write only elements with row >= col + diag
   int diag = 0;
   int shadow_acc = 0;        // 16-bit copy of alpha*op(A)op(B) alone (not of D)
+  int round_prod = 0;        // D = beta*C + fp32(fp16(alpha*op(A)op(B))): D holds the product's 16-bit value
 };
 
 struct GemmCall {
@@ -75,7 +76,7 @@ struct GemmCall {
   Op16 A, B;
   float alpha = 1.f, beta = 0.f;
   GemmOut out;
-  int prec = LATER_PREC_FP16;       // operand format of A and B
+  int prec = LATER_PREC_FP16;       // operand format of A and B (SPLIT2: A hi+lo, B hi)
   int out_prec = LATER_PREC_FP16;   // format of Dh / Dl
 };
 

@@ -374,6 +374,7 @@ later_status_t ls_solve(cudaStream_t st, int m, int n, int k, const float* A, in
   note_launch();
   info->factor_precision = o.prec;
   Options os = o;  // the solves with R run in FP32 (n <= 256) or the factorisation's precision
+  if (os.prec == LATER_PREC_SPLIT2) os.prec = LATER_PREC_FP16;  // SPLIT2 is a QR-only mode
   auto apply = [&](const float* V /*m x k*/) -> later_status_t {
     // v32[:n] = Q^T V, then R x = v  <=>  L^T x = v with L = R^T
     LATER_CHECK(simt_tn(st, m, n, k, w.F, m, V, m, w.v32, n, 0, pa, 1.f));

@@ -122,6 +122,10 @@ def rgsqrf(A: np.ndarray, leaf: int = 128, prec: str = "fp16", cgs2: bool = Fals
 
     Returns (Q, R) in FP32. Trailing update: R12 = Q1^T A2 (FP16 GemmEx, :45-49),
     A2 -= Q1 fp16(R12) (:51-56); R12 itself is kept in FP32.
+
+    prec "split2" (no reference counterpart): R12 = fp16(Q1)^T fp16(A2) kept at
+    its FP16-rounded value, and A2 -= (Q1hi + Q1lo/2^11) fp16(R12), so the
+    factor that is subtracted is the one stored (backward error at FP32 level).
     """
     a = np.array(A, dtype=F32, order="F")
     m, n = a.shape
@@ -138,6 +142,13 @@ def rgsqrf(A: np.ndarray, leaf: int = 128, prec: str = "fp16", cgs2: bool = Fals
         passes = 2 if cgs2 else 1
         r12 = np.zeros((n1, nn - n1), dtype=F32)
         for _ in range(passes):
+            if prec == "split2":
+                s = round16(round16(q1.T) @ round16(a[:, n1:]))
+                qh = round16(q1)
+                ql = ((q1 - qh) * F32(2048)).astype(np.float16).astype(F32)
+                r12 += s
+                a[:, n1:] -= qh @ s + (ql @ s) * F32(1.0 / 2048)
+                continue
             s = tc_gemm(q1.T, a[:, n1:], prec)
             r12 += s
             a[:, n1:] -= tc_gemm(q1, s, prec)

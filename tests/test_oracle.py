@@ -31,6 +31,16 @@ def test_rgsqrf_oracle_fp16_error_model():
     assert 1e-5 < e < 5e-4
 
 
+def test_rgsqrf_oracle_split2_error_model():
+    # split2: the subtracted R12 is the stored one and Q1 enters the update as hi + lo, so the
+    # backward error drops to the FP32 level while orthogonality stays at the FP16 level.
+    A = gen.normal(2048, 512, seed=1)
+    Q2, R2 = lo.rgsqrf(A, prec="split2")
+    Qh, Rh = lo.rgsqrf(A, prec="fp16")
+    assert metrics.qr_backward_error(A, Q2, R2) < 1e-6
+    assert metrics.orthogonality(Q2) < 2 * metrics.orthogonality(Qh) + 1e-6
+
+
 def test_mgs_block_and_tsqr_agree():
     A = gen.normal(2000, 32, seed=5)
     q1, r1 = lo.mgs_block(A)

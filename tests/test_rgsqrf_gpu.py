@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 # Accuracy bounds per precision (FP64-measured). The GPU result must be within
 # a factor FACTOR of the oracle's own figure and below the absolute bound.
 FACTOR = 3.0
-BOUND_BWD = {"fp16": 5e-4, "bf16": 4e-3, "split3": 2e-6}
+BOUND_BWD = {"fp16": 5e-4, "bf16": 4e-3, "split3": 2e-6, "split2": 2e-6}
 
 
 def run_gpu(A, **kw):
@@ -30,6 +30,9 @@ def run_gpu(A, **kw):
     (1000, 256, 32, "fp16", False),
     (3001, 384, 128, "bf16", False),
     (2048, 512, 128, "split3", False),
+    (4096, 1024, 128, "split2", False),
+    (1000, 256, 32, "split2", False),
+    (2048, 512, 128, "split2", True),
     (2048, 512, 128, "fp16", True),
     (300, 96, 128, "fp16", False),
     (70000, 64, 64, "fp16", False),
@@ -45,7 +48,19 @@ def test_rgsqrf_matches_oracle(cuda, m, n, leaf, prec, cgs2):
     # R upper triangular with positive diagonal and zeros below; close to the oracle's R.
     assert np.all(np.tril(R, -1) == 0)
     assert np.all(np.diag(R) > 0)
-    assert np.linalg.norm(R - Ro) / np.linalg.norm(Ro) <= max(FACTOR * BOUND_BWD[prec], 1e-5)
+    # split2 keeps R12 at its FP16 value: R agrees with the oracle's to FP16 level, like fp16.
+    r_tol = FACTOR * BOUND_BWD["fp16"] if prec == "split2" else max(FACTOR * BOUND_BWD[prec], 1e-5)
+    assert np.linalg.norm(R - Ro) / np.linalg.norm(Ro) <= r_tol
+
+
+def test_split2_backward_error_at_fp32_level(cuda):
+    """split2 pays 1.5x the FP16 tensor work for an FP32-level backward error; FP16 stays near 1e-4."""
+    A = gen.svd_matrix(4096, 1024, 1e3, seed=21)
+    Q2, R2 = run_gpu(A, precision="split2")
+    Qh, Rh = run_gpu(A, precision="fp16")
+    b2, bh = metrics.qr_backward_error(A, Q2, R2), metrics.qr_backward_error(A, Qh, Rh)
+    assert b2 <= 2e-6 and bh >= 20 * b2, (b2, bh)
+    assert metrics.orthogonality(Q2) <= 2 * metrics.orthogonality(Qh) + 1e-5
 
 
 def test_rgsqrf_uniform_reference_input(cuda):
