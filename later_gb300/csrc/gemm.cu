@@ -37,13 +37,18 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int BK = 64;
+// Warp 0 lane 0 issues the TMA loads, warp 1 lane 0 the MMAs (warp 1 owns the
+// TMEM allocation), warps 2..7 prefetch C into L2; then all eight warps run the
+// epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its lane quarter) and
+// the 32-column chunks c0 = 32 (w / 4), + 64, ... of the tile.
+constexpr int kGemmThreads = 256;
 constexpr float kLoScale = 2048.f;       // SPLIT3 lo operands are stored scaled by 2^11
 constexpr float kLoScaleInv = 1.f / 2048.f;
 
 struct GemmArgs {
   int M, N, K;
   int kb_total, kb_per_split, splits;
-  int tiles_m;
+  int tiles_m, tiles_n;
   float alpha, beta;
   const float* C;
   int64_t ldc;
@@ -62,6 +67,20 @@ struct GemmArgs {
   int* status;
   long long budget;
 };
+
+// Output tile of linear index t, in groups of kGroupM tile rows: inside a
+// group the row index varies fastest, so the CTAs resident at one time cover
+// about kGroupM x (CTAs / kGroupM) tiles and share their A row panels and B
+// column panels through L2 instead of each streaming its own A panel from HBM.
+constexpr int kGroupM = 16;
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int* tm, int* tn) {
+  const int per_group = kGroupM * tiles_n;
+  const int first_m = (t / per_group) * kGroupM;
+  const int rows = min(tiles_m - first_m, kGroupM);
+  const int r = t % per_group;
+  *tm = first_m + r % rows;
+  *tn = r / rows;
+}
 
 __device__ __forceinline__ void store16(void* base, int64_t idx, float v, int bf16) {
   if (bf16)
@@ -97,6 +116,48 @@ __device__ __forceinline__ void epilogue_store_c(const GemmArgs& p, int row, int
 
 // SPL: 0 one product; 1 A split (hi.hi into accumulator 0, lo.hi into 1);
 // 2 both split, SPLIT3 (hi.hi into 0, hi.lo + lo.hi into 1).
+// Epilogue of 32 interior elements of one row (columns col0 .. col0 + 31, all
+// inside the output, no triangle): the same arithmetic as epilogue_store_c
+// with the mode tests hoisted out of the element loop.
+__device__ __forceinline__ void epilogue_chunk(const GemmArgs& p, int row, int col0, const float (&acc)[32],
+                                               const float (&c)[32]) {
+  float prod[32], val[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    prod[j] = p.alpha * acc[j];
+    if (p.round_prod) prod[j] = __half2float(__float2half_rn(prod[j]));
+    val[j] = p.beta != 0.f ? prod[j] + p.beta * c[j] : prod[j];
+  }
+  float* d = p.D + row + static_cast<int64_t>(col0) * p.ldd;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) d[j * p.ldd] = val[j];
+  if (!p.Dh) return;
+  const float* src = p.shadow_acc ? prod : val;
+  const int64_t h0 = row + static_cast<int64_t>(col0) * p.ldh;
+  if (p.out_mode == 1) {
+    __nv_bfloat16* h = reinterpret_cast<__nv_bfloat16*>(p.Dh) + h0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) h[j * p.ldh] = __float2bfloat16_rn(src[j]);
+    return;
+  }
+  __half* h = reinterpret_cast<__half*>(p.Dh) + h0;
+  bool big = false;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    big |= fabsf(src[j]) > 65504.f;
+    h[j * p.ldh] = __float2half_rn(src[j]);
+  }
+  if (big) report(p.status, DEV_RANGE);
+  if (p.out_mode == 2) {
+    __half* l = reinterpret_cast<__half*>(p.Dl) + h0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const float hv = __half2float(__float2half_rn(src[j]));
+      l[j * p.ldh] = __float2half_rn((src[j] - hv) * kLoScale);
+    }
+  }
+}
+
 template <int BN, bool A_MN, bool B_MN, int SPL, int STAGES>
 struct Cfg {
   static constexpr int A_BYTES = BM * BK * 2;  // 16 KB
@@ -109,7 +170,7 @@ struct Cfg {
 };
 
 template <int BN, bool A_MN, bool B_MN, int SPL, int STAGES>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kGemmThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const __grid_constant__ CUtensorMap tmAl, const __grid_constant__ CUtensorMap tmBl,
                    const GemmArgs p) {
@@ -126,8 +187,8 @@ __global__ void __launch_bounds__(128, 1)
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const int tile_m = blockIdx.x % p.tiles_m;
-  const int tile_n = blockIdx.x / p.tiles_m;
+  int tile_m, tile_n;
+  tile_coords(blockIdx.x, p.tiles_m, p.tiles_n, &tile_m, &tile_n);
   const int split = blockIdx.y;
   const int m0 = tile_m * BM;
   const int n0 = tile_n * BN;
@@ -239,6 +300,18 @@ __global__ void __launch_bounds__(128, 1)
       }
       tc_commit(done);  // arrives once every MMA above has completed
     }
+  } else if (p.beta != 0.f && p.splits == 1) {
+    // Warps 2-3 are idle during the mainloop: pull this tile's C block into L2
+    // so that the epilogue's reads of it hit L2 rather than HBM.
+    const int rows = min(BM, p.M - m0), ncols = min(BN, p.N - n0);
+    if (rows > 0 && ncols > 0) {
+      const int lines = (rows + 31) / 32;  // 128-byte lines of 32 floats per column
+      for (int e = threadIdx.x - 64; e < ncols * lines; e += kGemmThreads - 64) {
+        const int c = e / lines, l = e % lines;
+        const float* addr = p.C + m0 + 32 * l + static_cast<int64_t>(n0 + c) * p.ldc;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(addr));
+      }
+    }
   }
   __syncwarp();
 
@@ -248,14 +321,25 @@ __global__ void __launch_bounds__(128, 1)
   const bool ok = drained && (*abort_flag == 0) && nkb > 0;
   if (!ok && threadIdx.x == 0) report(p.status, DEV_TIMEOUT);
 
-  const int r = warp * 32 + lane;  // tile row == TMEM lane
+  const int quarter = warp & 3, half = warp >> 2;
+  const int r = quarter * 32 + lane;  // tile row == TMEM lane
   const int row = m0 + r;
-  const uint32_t t_row = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+  const uint32_t t_row = tmem + (static_cast<uint32_t>(quarter * 32) << 16);
   // Split-K: this CTA's FP32 partial tile, [col][row], reduced by splitk_reduce_kernel.
   float* mine = p.splits > 1 ? p.partial + (static_cast<int64_t>(blockIdx.x) * p.splits + split) * (BM * BN)
                              : nullptr;
+  // C values of a 32-column chunk are loaded one chunk ahead of the chunk's
+  // stores. C and D may alias: each element is read and written by the same
+  // thread, and a chunk's C is read before any of its D stores.
+  const bool rd = (p.beta != 0.f) && row < p.M && ok && !mine;
+  float cv[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const int col = n0 + 32 * half + j;
+    cv[j] = (rd && 32 * half < BN && col < p.N) ? p.C[row + static_cast<int64_t>(col) * p.ldc] : 0.f;
+  }
 #pragma unroll 1
-  for (int c0 = 0; c0 < BN; c0 += 32) {
+  for (int c0 = 32 * half; c0 < BN; c0 += 64) {
     float v[32];
     tmem_ld_32x32b_x32(t_row + c0, v);
     if (SPL) {
@@ -268,17 +352,20 @@ __global__ void __launch_bounds__(128, 1)
 #pragma unroll
       for (int j = 0; j < 32; ++j) __stcg(&mine[(c0 + j) * BM + r], ok ? v[j] : 0.f);
     } else if (ok) {
-      // C and D may alias: read the chunk's 32 C values before any store so the
-      // loads overlap instead of serialising behind the stores.
-      float cv[32];
-      const bool rd = (p.beta != 0.f) && row < p.M;
+      float cn[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        const int col = n0 + c0 + j;
-        cv[j] = (rd && col < p.N) ? p.C[row + static_cast<int64_t>(col) * p.ldc] : 0.f;
+        const int col = n0 + c0 + 64 + j;
+        cn[j] = (rd && c0 + 64 < BN && col < p.N) ? p.C[row + static_cast<int64_t>(col) * p.ldc] : 0.f;
+      }
+      if (row < p.M && n0 + c0 + 32 <= p.N && !p.lower) {
+        epilogue_chunk(p, row, n0 + c0, v, cv);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) epilogue_store_c(p, row, n0 + c0 + j, v[j], cv[j]);
       }
 #pragma unroll
-      for (int j = 0; j < 32; ++j) epilogue_store_c(p, row, n0 + c0 + j, v[j], cv[j]);
+      for (int j = 0; j < 32; ++j) cv[j] = cn[j];
     }
   }
 
@@ -298,7 +385,8 @@ __global__ void __launch_bounds__(256) splitk_reduce_kernel(const GemmArgs p) {
   const int rem = blockIdx.x % tiles_per_row_groups;
   const int rg = rem % (BM / 32);
   const int cg = rem / (BM / 32);
-  const int tile_m = tile % p.tiles_m, tile_n = tile / p.tiles_m;
+  int tile_m, tile_n;
+  tile_coords(tile, p.tiles_m, p.tiles_n, &tile_m, &tile_n);
   const int r = rg * 32 + threadIdx.x % 32;
   const int j = threadIdx.x / 32;
   const float* base = p.partial + static_cast<int64_t>(tile) * p.splits * (BM * BN);
@@ -350,7 +438,7 @@ later_status_t launch_cfg(const CUtensorMap& a, const CUtensorMap& b, const CUte
     LATER_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C_::SMEM));
     attr_done[dev] = true;
   }
-  kern<<<grid, 128, C_::SMEM, st>>>(a, b, al, bl, args);
+  kern<<<grid, kGemmThreads, C_::SMEM, st>>>(a, b, al, bl, args);
   note_launch();
   LATER_CHECK_CUDA(cudaGetLastError());
   if (args.splits > 1) {
@@ -435,6 +523,7 @@ later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, lon
   a.kb_per_split = kb_per_split;
   a.splits = splits;
   a.tiles_m = tiles_m;
+  a.tiles_n = tiles_n;
   a.alpha = g.alpha;
   a.beta = g.beta;
   a.C = g.out.C;
