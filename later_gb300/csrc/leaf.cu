@@ -491,6 +491,7 @@ struct ResPanelSmem {
   float rinv1[32];
   float rinv2[32];
   int ok;
+  int devbits;  // max |G2 - I| (float bits)
 };
 
 constexpr int MS = 132;   // row stride of the leaf-wide Gram / Cholesky factor (16-byte rows)
@@ -676,18 +677,26 @@ __device__ void slab_gemm_sub(float* D, int dc, const float* S0, int sc, const f
   }
 }
 
-// Y R = A for the slab rows (Y = columns 0 .. k-1 of `Y`, in place; R upper
-// k x k column-major in Rc): per block of 8 columns, each thread solves its
-// row's 8 x 8 diagonal block (a chain of 8), then the columns after the block
-// are updated by all threads as a small tiled product (no chain). Rt is a
+// Y R = A for the slab rows (Y = columns 0 .. k-1 of `Y`; A = columns
+// a0 .. a0 + k - 1 of the slab X, read by the first block and its update, so
+// A needs no copy; R upper k x k column-major in Rc): per block of 8 columns,
+// each thread solves its row's 8 x 8 diagonal block (a chain of 8), then the
+// columns after the block are updated by all threads as a small tiled product
+// (no chain). Y's padding rows [rows, rows_eff) come out zero. Rt is a
 // 8 x RCS scratch for the block's rows of R.
-__device__ void slab_solve(float* Y, int k, int rows, int rows_eff, const float* Rc, const float* rinv, float* Rt) {
+__device__ void slab_solve(float* Y, const float* X, int a0, int k, int rows, int rows_eff, const float* Rc,
+                           const float* rinv, float* Rt) {
   const int tid = threadIdx.x;
   for (int b = 0; b < k; b += 8) {
+    if (b == 0 && tid >= rows && tid < rows_eff) {
+#pragma unroll
+      for (int l = 0; l < 8; ++l) Y[l * XS + tid] = 0.f;
+    }
     if (tid < rows) {
+      const float* src = b == 0 ? X + a0 * XS : Y;
       float x[8];
 #pragma unroll
-      for (int l = 0; l < 8; ++l) x[l] = b + l < k ? Y[(b + l) * XS + tid] : 0.f;
+      for (int l = 0; l < 8; ++l) x[l] = b + l < k ? src[(b + l) * XS + tid] : 0.f;
 #pragma unroll
       for (int l = 0; l < 8; ++l) {
         if (b + l < k) {
@@ -709,7 +718,10 @@ __device__ void slab_solve(float* Y, int k, int rows, int rows_eff, const float*
     }
     __syncthreads();
     if (nj > 0) {
-      slab_gemm_sub(Y, b + 8, Y, b + 8, Y, b, 8, Rt, RCS, nj, rows_eff);
+      if (b == 0)
+        slab_gemm_sub(Y, 8, X, a0 + 8, Y, 0, 8, Rt, RCS, nj, rows_eff);
+      else
+        slab_gemm_sub(Y, b + 8, Y, b + 8, Y, b, 8, Rt, RCS, nj, rows_eff);
       __syncthreads();
     }
   }
@@ -733,12 +745,8 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
   __syncthreads();
   if (!ps.ok) return res_fallback(P, S, gs, okflag, c0, k, r0, rows);
   // ---- Y = X R1^-1 (rows of the slab), G2 = Y^T Y
-  for (int e = tid; e < 32 * rows_eff; e += LT) {
-    const int c = e / rows_eff, r = e % rows_eff;
-    S.Y[c * XS + r] = c < k ? S.X[(c0 + c) * XS + r] : 0.f;
-  }
-  __syncthreads();
-  slab_solve(S.Y, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2);
+  slab_solve(S.Y, S.X, c0, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2);
+  if (tid == 0) ps.devbits = 0;
   res_tn(S.Y, 0, k, S.Y, 0, k, rows_eff, S.gp, P.part);
   if (!grid_barrier(gs, okflag)) return false;
   reduce_partials(P.part, k, k, 64, [&](int e, float v) { P.red[e] = v; });
@@ -751,16 +759,22 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
   // F = triu(E) - diag(E) / 2, and Q = Y (I - F) has Q^T Q = I + O(E^2) and
   // Q (I + F) R1 = Y R1 + O(E^2): no second Cholesky and no second
   // substitution chain, only a small product. Otherwise the exact path.
-  if (tid < 32) {
+  // max |E| over all threads (a NaN entry counts as a large deviation).
+  {
     float dev = 0.f;
-    for (int j = 0; j < k; ++j)
-      if (tid < k) dev = fmaxf(dev, fabsf(ps.G[tid * 33 + j] - (j == tid ? 1.f : 0.f)));
+    for (int e = tid; e < 1024; e += LT) {
+      const int i = e / 32, j = e % 32;
+      if (i < k && j < k) {
+        const float d = fabsf(ps.G[i * 33 + j] - (i == j ? 1.f : 0.f));
+        dev = d <= dev ? dev : (d == d ? d : 1.f);
+      }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) dev = fmaxf(dev, __shfl_xor_sync(0xffffffffu, dev, o));
-    if (tid == 0) ps.ok = dev <= 3e-4f ? 2 : 0;
+    if ((tid & 31) == 0) atomicMax(&ps.devbits, __float_as_int(dev));
   }
   __syncthreads();
-  const bool first_order = ps.ok == 2;
+  const bool first_order = __int_as_float(ps.devbits) <= 3e-4f;
   if (first_order) {
     // F row-major (stride RCS) in R2's place
     for (int e = tid; e < 32 * RCS; e += LT) {
@@ -783,9 +797,10 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
       if (r < rows) S.X[(c0 + c) * XS + r] = S.Y[c * XS + r];
     }
   }
-  // R = R2 R1 (exact) or (I + F) R1 (first order)
-  if (blockIdx.x == 0) {
-    for (int e = tid; e < 1024; e += LT) {
+  // R = R2 R1 (exact) or (I + F) R1 (first order); every CTA holds both
+  // factors, the 1024 entries go to the first four CTAs (one per thread)
+  {
+    for (int e = static_cast<int>(blockIdx.x) * LT + tid; e < 1024; e += static_cast<int>(gridDim.x) * LT) {
       const int i = e % 32, j = e / 32;
       if (i < k && j < k) {
         float sum = 0.f;
