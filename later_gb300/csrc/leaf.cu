@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 
 #include "dense_dev.cuh"
 #include "leaf.cuh"
@@ -45,7 +46,7 @@ constexpr int PART = 8448;  // floats per CTA partial: 64 x 64 (i + 64 j), or a 
 constexpr int kMaxSteps = 8;
 
 struct LeafStep {
-  int kind;  // 0: panel (c0, w1 columns); 1: update
+  int kind;  // 0: panel (c0, w1 columns); 1: update; 2: panel that also projects columns [c1, c1 + w2)
   int c0, w1, c1, w2;
 };
 
@@ -483,6 +484,7 @@ __device__ bool update_step(const LeafPlan& P, LeafSmem& sm, GridSync& gs, int* 
 // was.
 constexpr int RMAX = 256;
 constexpr int XS = RMAX + 4;
+constexpr int PMS = 100;  // row stride of the 32 x (<= 96) projection block C (16-byte rows)
 
 struct ResPanelSmem {
   float G[32 * 33];
@@ -504,7 +506,10 @@ struct ResSmem {
       float Y[32 * XS];
       float gp[4096];  // per-row-group partial products
       union {
-        ResPanelSmem p;
+        struct {
+          ResPanelSmem p;
+          alignas(16) float Pm[32 * PMS];  // Y^T A_rest, then C = Q^T A_rest (row-major, float4 rows)
+        };
         float Ps[64 * SP];  // P = Q^T A2, row-major
         TsqrReduceSmem tr;
         TsqrApplySmem ta;
@@ -519,6 +524,10 @@ struct ResSmem {
     };
   };
 };
+
+static_assert(sizeof(ResSmem) <= 227 * 1024, "resident leaf shared memory exceeds the per-CTA limit");
+static_assert(offsetof(ResSmem, Pm) % 16 == 0 && offsetof(ResSmem, Ps) % 16 == 0 && offsetof(ResSmem, Y) % 16 == 0,
+              "float4 tiles need 16-byte alignment");
 
 // Loads rows [r0, r0 + rows) of the leaf's w columns into X; rows [rows, rows rounded up to 4)
 // are zeroed (the phases read whole row quads).
@@ -588,8 +597,11 @@ __device__ void res_store(const LeafPlan& P, const float* X, int r0, int rows, i
 // Xb = columns [b0, b0 + nb) of `Xb`, na, nb <= 64) into part (entry i + 64 j).
 // Threads form row groups when the output needs fewer than 256 4x4 tiles; the
 // groups' sums are added in group order.
-__device__ void res_tn(const float* Xa, int a0, int na, const float* Xb, int b0, int nb, int rows_eff, float* gp,
-                       float* part) {
+// Optional second B buffer: B's columns c >= nb1 are columns b20 + c - nb1 of
+// Xb2 (so [Y | X_rest] is one operand); nb up to 128 (at most 256 4x4 tiles).
+template <class Emit>
+__device__ void res_tn_emit(const float* Xa, int a0, int na, const float* Xb, int b0, int nb, int rows_eff,
+                            float* gp, Emit emit, const float* Xb2 = nullptr, int b20 = 0, int nb1 = 1 << 30) {
   const int tid = threadIdx.x;
   const int nta = (na + 3) / 4, ntb = (nb + 3) / 4, nt = nta * ntb;
   const int groups = max(1, LT / nt);
@@ -603,14 +615,19 @@ __device__ void res_tn(const float* Xa, int a0, int na, const float* Xb, int b0,
     // thread (ti, tj) owns columns ti + nta u of Xa and tj + ntb v of Xb: with XS = 4 x odd,
     // the eight float4 rows a warp reads at once fall in eight different bank groups
     const float* pa = Xa + (a0 + ti) * XS;
-    const float* pb = Xb + (b0 + tj) * XS;
+    const float* pbv[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int c = tj + ntb * v;  // padded columns (c >= nb) read a valid column; their sums are unused
+      pbv[v] = c < nb1 ? Xb + (b0 + c) * XS : Xb2 + min(b20 + c - nb1, kLeafMaxWidth - 1) * XS;
+    }
 #pragma unroll 2
     for (int r = rb; r < re; r += 4) {
       float4 a[4], b[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) a[u] = *reinterpret_cast<const float4*>(&pa[u * nta * XS + r]);
 #pragma unroll
-      for (int v = 0; v < 4; ++v) b[v] = *reinterpret_cast<const float4*>(&pb[v * ntb * XS + r]);
+      for (int v = 0; v < 4; ++v) b[v] = *reinterpret_cast<const float4*>(&pbv[v][r]);
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -623,12 +640,18 @@ __device__ void res_tn(const float* Xa, int a0, int na, const float* Xb, int b0,
       for (int v = 0; v < 4; ++v) gp[g * npad + (ti + nta * u) + 4 * nta * (tj + ntb * v)] = acc[u][v];
   }
   __syncthreads();
-  float* p = part + static_cast<int64_t>(blockIdx.x) * PART;
   for (int e = tid; e < npad; e += LT) {
     float s = 0.f;
     for (int gg = 0; gg < groups; ++gg) s += gp[gg * npad + e];
-    p[e % (4 * nta) + 64 * (e / (4 * nta))] = s;
+    emit(e % (4 * nta), e / (4 * nta), s);
   }
+}
+
+// res_tn_emit with the sums written to this CTA's partial block (entry i + 64 j).
+__device__ void res_tn(const float* Xa, int a0, int na, const float* Xb, int b0, int nb, int rows_eff, float* gp,
+                       float* part) {
+  float* p = part + static_cast<int64_t>(blockIdx.x) * PART;
+  res_tn_emit(Xa, a0, na, Xb, b0, nb, rows_eff, gp, [&](int i, int j, float v) { p[i + 64 * j] = v; });
 }
 
 // Panel fallback: the slab's columns [c0, c0 + k) go back to A, MGS-TSQR runs
@@ -727,8 +750,29 @@ __device__ void slab_solve(float* Y, const float* X, int a0, int k, int rows, in
   }
 }
 
+__device__ bool res_update(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, const LeafStep& s, int rows,
+                           int pass);
+
+// After a fallback panel: the columns [rest0, rest0 + nrest) are projected by
+// separate update steps (at most 64 columns each).
+__device__ bool res_project_rest(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, int c0, int k,
+                                 int rest0, int nrest, int rows) {
+  for (int j0 = 0; j0 < nrest; j0 += 64) {
+    __syncthreads();
+    if (!res_update(P, S, gs, okflag, LeafStep{1, c0, k, rest0 + j0, min(64, nrest - j0)}, rows, 0)) return false;
+  }
+  return true;
+}
+
+// One 32-column panel by CholQR2 (first-order second pass when G2 is within
+// 3e-4 of I). With nrest > 0 (right-looking steps, full 32-column panel), the
+// second reduction also carries P = Y^T A_rest for the leaf's later columns
+// [rest0, rest0 + nrest): the panel's projection C = Q^T A_rest follows
+// locally, C = (I - F)^T P (first order) or R2^-T P (exact), then A_rest -=
+// Q C and R[panel, rest] = C. One reduction fewer per later column block than
+// a separate update step.
 __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, int c0, int k, int r0,
-                          int rows) {
+                          int rows, int rest0, int nrest) {
   ResPanelSmem& ps = S.p;
   const int tid = threadIdx.x;
   const int rows_eff = (rows + 3) & ~3;
@@ -743,17 +787,38 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
   __syncthreads();
   chol_upper(ps.G, k, ps.R1, ps.rinv1, false, &ps.ok);
   __syncthreads();
-  if (!ps.ok) return res_fallback(P, S, gs, okflag, c0, k, r0, rows);
-  // ---- Y = X R1^-1 (rows of the slab), G2 = Y^T Y
+  if (!ps.ok)
+    return res_fallback(P, S, gs, okflag, c0, k, r0, rows) &&
+           res_project_rest(P, S, gs, okflag, c0, k, rest0, nrest, rows);
+  // ---- Y = X R1^-1 (rows of the slab), G2 = Y^T Y (and P = Y^T A_rest)
   slab_solve(S.Y, S.X, c0, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2);
   if (tid == 0) ps.devbits = 0;
-  res_tn(S.Y, 0, k, S.Y, 0, k, rows_eff, S.gp, P.part);
-  if (!grid_barrier(gs, okflag)) return false;
-  reduce_partials(P.part, k, k, 64, [&](int e, float v) { P.red[e] = v; });
-  if (!grid_barrier(gs, okflag)) return false;
-  batched_copy(
-      1024, [&](int e) { return ((e % 32) < k && (e / 32) < k) ? __ldcg(&P.red[(e % 32) + 64 * (e / 32)]) : 0.f; },
-      [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
+  if (nrest == 0) {
+    res_tn(S.Y, 0, k, S.Y, 0, k, rows_eff, S.gp, P.part);
+    if (!grid_barrier(gs, okflag)) return false;
+    reduce_partials(P.part, k, k, 64, [&](int e, float v) { P.red[e] = v; });
+    if (!grid_barrier(gs, okflag)) return false;
+    batched_copy(
+        1024, [&](int e) { return ((e % 32) < k && (e / 32) < k) ? __ldcg(&P.red[(e % 32) + 64 * (e / 32)]) : 0.f; },
+        [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
+  } else {
+    // partial of [Y^T Y | Y^T A_rest], entry (i, j) at i + 32 j (k = 32)
+    float* prt = P.part + static_cast<int64_t>(blockIdx.x) * PART;
+    res_tn_emit(
+        S.Y, 0, 32, S.Y, 0, 32 + nrest, rows_eff, S.gp, [&](int i, int j, float v) { prt[i + 32 * j] = v; }, S.X,
+        rest0, 32);
+    if (!grid_barrier(gs, okflag)) return false;
+    reduce_partials(P.part, 32, 32 + nrest, 32, [&](int e, float v) { P.red[e] = v; });
+    if (!grid_barrier(gs, okflag)) return false;
+    batched_copy(
+        1024 + 32 * nrest, [&](int e) { return __ldcg(&P.red[e]); },
+        [&](int e, float v) {
+          if (e < 1024)
+            ps.G[(e % 32) * 33 + e / 32] = v;
+          else
+            S.Pm[(e % 32) * PMS + (e - 1024) / 32] = v;
+        });
+  }
   __syncthreads();
   // G2 = I + E. When max |E| <= 3e-4, chol(I + E) = I + F + O(E^2) with
   // F = triu(E) - diag(E) / 2, and Q = Y (I - F) has Q^T Q = I + O(E^2) and
@@ -788,7 +853,9 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
   } else {
     chol_upper(ps.G, k, ps.R2, ps.rinv2, true, &ps.ok);
     __syncthreads();
-    if (!ps.ok) return res_fallback(P, S, gs, okflag, c0, k, r0, rows);
+    if (!ps.ok)
+      return res_fallback(P, S, gs, okflag, c0, k, r0, rows) &&
+             res_project_rest(P, S, gs, okflag, c0, k, rest0, nrest, rows);
     // ---- Q = Y R2^-1 into the slab
     if (tid < rows) rows_solve(S.Y, XS, k, tid, ps.R2, ps.rinv2);
     __syncthreads();
@@ -796,6 +863,60 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
       const int c = e / rows_eff, r = e % rows_eff;
       if (r < rows) S.X[(c0 + c) * XS + r] = S.Y[c * XS + r];
     }
+  }
+  if (nrest > 0) {
+    // C = Q^T A_rest from P = Y^T A_rest. First order: C = (I - F)^T P = P - F^T P
+    // (F upper, row-major in R2) as 4 x 4 tiles, one per thread (8 x 24 at most),
+    // written back over P after a barrier. Exact: C = R2^-T P (R2 column-major),
+    // forward substitution per column in place.
+    const int nct = (nrest + 3) / 4;
+    const int it = tid % 8, jt = tid / 8;
+    const bool mine = first_order && tid < 8 * nct;
+    float cv[4][4];
+    if (mine) {
+      float acc[4][4] = {};
+#pragma unroll 4
+      for (int l = 0; l < 32; ++l) {
+        const float4 f = *reinterpret_cast<const float4*>(&ps.R2[l * RCS + 4 * it]);
+        const float4 q = *reinterpret_cast<const float4*>(&S.Pm[l * PMS + 4 * jt]);
+        const float fv[4] = {f.x, f.y, f.z, f.w};
+        const float qv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(fv[u], qv[v], acc[u][v]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4 q = *reinterpret_cast<const float4*>(&S.Pm[(4 * it + u) * PMS + 4 * jt]);
+        cv[u][0] = q.x - acc[u][0];
+        cv[u][1] = q.y - acc[u][1];
+        cv[u][2] = q.z - acc[u][2];
+        cv[u][3] = q.w - acc[u][3];
+      }
+    }
+    if (!first_order) {
+      for (int j = tid; j < nrest; j += LT) {
+        for (int i = 0; i < 32; ++i) {
+          float v = S.Pm[i * PMS + j];
+          for (int l = 0; l < i; ++l) v = fmaf(-ps.R2[i * RCS + l], S.Pm[l * PMS + j], v);
+          S.Pm[i * PMS + j] = v * ps.rinv2[i];
+        }
+      }
+    }
+    __syncthreads();
+    if (mine) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        *reinterpret_cast<float4*>(&S.Pm[(4 * it + u) * PMS + 4 * jt]) =
+            make_float4(cv[u][0], cv[u][1], cv[u][2], cv[u][3]);
+    }
+    __syncthreads();
+    const int n = 32 * nrest;
+    // A_rest -= Q C; R[panel, rest] = C (spread over the CTAs)
+    slab_gemm_sub(S.X, rest0, S.X, rest0, S.X, c0, 32, S.Pm, PMS, nrest, rows_eff);
+    for (int e = static_cast<int>(blockIdx.x) * LT + tid; e < n; e += static_cast<int>(gridDim.x) * LT)
+      P.R[(c0 + e % 32) + static_cast<int64_t>(rest0 + e / 32) * P.ldr] = S.Pm[(e % 32) * PMS + e / 32];
   }
   // R = R2 R1 (exact) or (I + F) R1 (first order); every CTA holds both
   // factors, the 1024 entries go to the first four CTAs (one per thread)
@@ -1129,8 +1250,8 @@ __global__ void __launch_bounds__(LT, 1) leaf_res_kernel(LeafPlan P) {
   for (int i = 0; i < P.nsteps && ok && !done; ++i) {
     const LeafStep s = P.step[i];
     __syncthreads();
-    if (s.kind == 0) {
-      ok = res_panel(P, S, gs, &okflag, s.c0, s.w1, r0, rows);
+    if (s.kind == 0 || s.kind == 2) {
+      ok = res_panel(P, S, gs, &okflag, s.c0, s.w1, r0, rows, s.c1, s.kind == 2 ? s.w2 : 0);
     } else {
       ok = res_update(P, S, gs, &okflag, s, rows, 0);
       if (ok && P.cgs2) ok = res_update(P, S, gs, &okflag, s, rows, 1);
@@ -1180,6 +1301,15 @@ __global__ void __launch_bounds__(LT, 1) leaf_kernel(LeafPlan P) {
       atomicExch(P.sync + 2, 0);
       atomicExch(P.sync + 1, 0);
     }
+  }
+}
+
+// Right-looking steps for the resident kernel without CGS2: one step per
+// 32-column panel, each projecting all later columns of the leaf.
+void build_steps_rl(int w, LeafPlan* P) {
+  for (int c0 = 0; c0 < w; c0 += 32) {
+    const int k = std::min(32, w - c0);
+    P->step[P->nsteps++] = LeafStep{2, c0, k, c0 + k, w - c0 - k};
   }
 }
 
@@ -1267,7 +1397,10 @@ later_status_t leaf_fused(cudaStream_t st, int m, int w, float* A, int64_t lda, 
   P.wide = try_wide && resident && w > 32 && !cgs2;
   P.cgs2 = cgs2;
   P.mode = out_prec == LATER_PREC_BF16 ? 1 : (out_prec == LATER_PREC_SPLIT3 ? 2 : 0);
-  build_steps(w, 0, &P);
+  if (resident && !cgs2)
+    build_steps_rl(w, &P);
+  else
+    build_steps(w, 0, &P);
   P.A = A;
   P.lda = lda;
   P.R = R;
