@@ -504,7 +504,8 @@ struct ResSmem {
   union {
     struct {  // 32-column panels
       float Y[32 * XS];
-      float gp[4096];  // per-row-group partial products
+      float Hn[32 * 33];  // the next panel's Gram matrix before this panel's update (right-looking steps)
+      float gp[4096];     // per-row-group partial products
       union {
         struct {
           ResPanelSmem p;
@@ -767,23 +768,41 @@ __device__ bool res_project_rest(const LeafPlan& P, ResSmem& S, GridSync& gs, in
 // One 32-column panel by CholQR2 (first-order second pass when G2 is within
 // 3e-4 of I). With nrest > 0 (right-looking steps, full 32-column panel), the
 // second reduction also carries P = Y^T A_rest for the leaf's later columns
-// [rest0, rest0 + nrest): the panel's projection C = Q^T A_rest follows
-// locally, C = (I - F)^T P (first order) or R2^-T P (exact), then A_rest -=
-// Q C and R[panel, rest] = C. One reduction fewer per later column block than
-// a separate update step.
+// [rest0, rest0 + nrest) and H = A_next^T A_next for the next panel's columns
+// (the first kn of them, before this panel's update): the projection C =
+// Q^T A_rest follows locally, C = (I - F)^T P (first order) or R2^-T P
+// (exact), then A_rest -= Q C and R[panel, rest] = C; and the next panel's
+// first-pass Gram matrix is H - C_next^T C_next (the update removes exactly
+// the component along the orthonormal Q), so that panel skips its first
+// reduction (*h_out; its second CholQR pass runs on the data as always).
 __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, int c0, int k, int r0,
-                          int rows, int rest0, int nrest) {
+                          int rows, int rest0, int nrest, bool h_in, bool* h_out) {
   ResPanelSmem& ps = S.p;
   const int tid = threadIdx.x;
   const int rows_eff = (rows + 3) & ~3;
+  *h_out = false;
   // ---- G = A^T A
-  res_tn(S.X, c0, k, S.X, c0, k, rows_eff, S.gp, P.part);
-  if (!grid_barrier(gs, okflag)) return false;
-  reduce_partials(P.part, k, k, 64, [&](int e, float v) { P.red[e] = v; });
-  if (!grid_barrier(gs, okflag)) return false;
-  batched_copy(
-      1024, [&](int e) { return ((e % 32) < k && (e / 32) < k) ? __ldcg(&P.red[(e % 32) + 64 * (e / 32)]) : 0.f; },
-      [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
+  if (h_in) {
+    // H - C^T C with C the previous panel's projection block of these columns (rows of Pm)
+    for (int e = tid; e < 1024; e += LT) {
+      const int i = e % 32, j = e / 32;
+      float v = 0.f;
+      if (i < k && j < k) {
+        v = S.Hn[i * 33 + j];
+#pragma unroll 8
+        for (int l = 0; l < 32; ++l) v = fmaf(-S.Pm[l * PMS + i], S.Pm[l * PMS + j], v);
+      }
+      ps.G[i * 33 + j] = v;
+    }
+  } else {
+    res_tn(S.X, c0, k, S.X, c0, k, rows_eff, S.gp, P.part);
+    if (!grid_barrier(gs, okflag)) return false;
+    reduce_partials(P.part, k, k, 64, [&](int e, float v) { P.red[e] = v; });
+    if (!grid_barrier(gs, okflag)) return false;
+    batched_copy(
+        1024, [&](int e) { return ((e % 32) < k && (e / 32) < k) ? __ldcg(&P.red[(e % 32) + 64 * (e / 32)]) : 0.f; },
+        [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
+  }
   __syncthreads();
   chol_upper(ps.G, k, ps.R1, ps.rinv1, false, &ps.ok);
   __syncthreads();
@@ -803,20 +822,28 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
         [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
   } else {
     // partial of [Y^T Y | Y^T A_rest], entry (i, j) at i + 32 j (k = 32)
+    // partial of [Y^T Y | Y^T A_rest | A_next^T A_next], entry (i, j) at i + 32 j (k = 32)
+    const int kn = min(32, nrest);
     float* prt = P.part + static_cast<int64_t>(blockIdx.x) * PART;
     res_tn_emit(
         S.Y, 0, 32, S.Y, 0, 32 + nrest, rows_eff, S.gp, [&](int i, int j, float v) { prt[i + 32 * j] = v; }, S.X,
         rest0, 32);
+    __syncthreads();  // gp is reused
+    res_tn_emit(S.X, rest0, kn, S.X, rest0, kn, rows_eff, S.gp,
+                [&](int i, int j, float v) { prt[i + 32 * (32 + nrest + j)] = v; });
     if (!grid_barrier(gs, okflag)) return false;
-    reduce_partials(P.part, 32, 32 + nrest, 32, [&](int e, float v) { P.red[e] = v; });
+    reduce_partials(P.part, 32, 32 + nrest + kn, 32, [&](int e, float v) { P.red[e] = v; });
     if (!grid_barrier(gs, okflag)) return false;
+    const int nh = 1024 + 32 * nrest;
     batched_copy(
-        1024 + 32 * nrest, [&](int e) { return __ldcg(&P.red[e]); },
+        nh + 32 * kn, [&](int e) { return __ldcg(&P.red[e]); },
         [&](int e, float v) {
           if (e < 1024)
             ps.G[(e % 32) * 33 + e / 32] = v;
-          else
+          else if (e < nh)
             S.Pm[(e % 32) * PMS + (e - 1024) / 32] = v;
+          else
+            S.Hn[(e % 32) * 33 + (e - nh) / 32] = v;
         });
   }
   __syncthreads();
@@ -917,6 +944,7 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
     slab_gemm_sub(S.X, rest0, S.X, rest0, S.X, c0, 32, S.Pm, PMS, nrest, rows_eff);
     for (int e = static_cast<int>(blockIdx.x) * LT + tid; e < n; e += static_cast<int>(gridDim.x) * LT)
       P.R[(c0 + e % 32) + static_cast<int64_t>(rest0 + e / 32) * P.ldr] = S.Pm[(e % 32) * PMS + e / 32];
+    *h_out = true;
   }
   // R = R2 R1 (exact) or (I + F) R1 (first order); every CTA holds both
   // factors, the 1024 entries go to the first four CTAs (one per thread)
@@ -1247,11 +1275,14 @@ __global__ void __launch_bounds__(LT, 1) leaf_res_kernel(LeafPlan P) {
       __syncthreads();
     }
   }
+  bool h_ready = false;  // the next panel's first-pass Gram matrix is already in smem
   for (int i = 0; i < P.nsteps && ok && !done; ++i) {
     const LeafStep s = P.step[i];
     __syncthreads();
     if (s.kind == 0 || s.kind == 2) {
-      ok = res_panel(P, S, gs, &okflag, s.c0, s.w1, r0, rows, s.c1, s.kind == 2 ? s.w2 : 0);
+      bool h_next = false;
+      ok = res_panel(P, S, gs, &okflag, s.c0, s.w1, r0, rows, s.c1, s.kind == 2 ? s.w2 : 0, h_ready, &h_next);
+      h_ready = h_next;
     } else {
       ok = res_update(P, S, gs, &okflag, s, rows, 0);
       if (ok && P.cgs2) ok = res_update(P, S, gs, &okflag, s, rows, 1);

@@ -121,6 +121,20 @@ def test_fused_leaf_matches_mgs_panels(cuda, m, n, prec, cgs2):
     assert metrics.orthogonality(Qf) <= 2 * metrics.orthogonality(Qm) + 1e-5
 
 
+@pytest.mark.parametrize("kappa,prec", [(1e3, "fp16"), (1e5, "fp16"), (1e5, "split3"), (1e5, "split2")])
+def test_fused_leaf_ill_conditioned(cuda, kappa, prec):
+    """SVD-constructed inputs (the precision sweep's construction): the fused leaf, whose right-looking
+    panels take their first-pass Gram matrix from the previous panel's reduction, keeps the backward
+    error and orthogonality of the reference's MGS-TSQR panels."""
+    A = gen.svd_matrix(4096, 512, kappa, seed=17)
+    Qf, Rf = run_gpu(A, precision=prec)
+    Qm, Rm = run_gpu(A, precision=prec, panel="mgs")
+    bf, bm = metrics.qr_backward_error(A, Qf, Rf), metrics.qr_backward_error(A, Qm, Rm)
+    assert bf <= max(2 * bm, 1e-6) and bf <= BOUND_BWD[prec], (bf, bm)
+    assert metrics.orthogonality(Qf) <= 2 * metrics.orthogonality(Qm) + 1e-5
+    assert np.all(np.tril(Rf, -1) == 0) and np.all(np.diag(Rf) > 0)
+
+
 def test_fused_leaf_falls_back_on_dependent_columns(cuda):
     """Exactly dependent columns inside a 32-column panel break CholQR2 (a non-positive pivot, or a
     second Gram matrix far from I); that panel is factored by MGS-TSQR inside the same launch."""
