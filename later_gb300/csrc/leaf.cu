@@ -674,9 +674,9 @@ __device__ bool res_fallback(const LeafPlan& P, ResSmem& S, GridSync& gs, int* o
 // over the slab's rows (P row-major with stride ldp in shared memory; D may be
 // S0). 4 rows x 4 columns per tile, float4 along rows.
 __device__ void slab_gemm_sub(float* D, int dc, const float* S0, int sc, const float* Sq, int qc, int K,
-                              const float* Pm, int ldp, int nj, int rows_eff) {
+                              const float* Pm, int ldp, int nj, int rows_eff, int t0 = -1, int nthr = LT) {
   const int nrt = rows_eff / 4, nct = (nj + 3) / 4;
-  for (int t = threadIdx.x; t < nrt * nct; t += LT) {
+  for (int t = t0 < 0 ? static_cast<int>(threadIdx.x) : t0; t < nrt * nct; t += nthr) {
     const int rt = t % nrt, ct = t / nrt;
     float acc[4][4] = {};
 #pragma unroll 4
@@ -697,56 +697,6 @@ __device__ void slab_gemm_sub(float* D, int dc, const float* S0, int sc, const f
         *reinterpret_cast<float4*>(&D[(dc + 4 * ct + v) * XS + 4 * rt]) =
             make_float4(x.x - acc[0][v], x.y - acc[1][v], x.z - acc[2][v], x.w - acc[3][v]);
       }
-    }
-  }
-}
-
-// Y R = A for the slab rows (Y = columns 0 .. k-1 of `Y`; A = columns
-// a0 .. a0 + k - 1 of the slab X, read by the first block and its update, so
-// A needs no copy; R upper k x k column-major in Rc): per block of 8 columns,
-// each thread solves its row's 8 x 8 diagonal block (a chain of 8), then the
-// columns after the block are updated by all threads as a small tiled product
-// (no chain). Y's padding rows [rows, rows_eff) come out zero. Rt is a
-// 8 x RCS scratch for the block's rows of R.
-__device__ void slab_solve(float* Y, const float* X, int a0, int k, int rows, int rows_eff, const float* Rc,
-                           const float* rinv, float* Rt) {
-  const int tid = threadIdx.x;
-  for (int b = 0; b < k; b += 8) {
-    if (b == 0 && tid >= rows && tid < rows_eff) {
-#pragma unroll
-      for (int l = 0; l < 8; ++l) Y[l * XS + tid] = 0.f;
-    }
-    if (tid < rows) {
-      const float* src = b == 0 ? X + a0 * XS : Y;
-      float x[8];
-#pragma unroll
-      for (int l = 0; l < 8; ++l) x[l] = b + l < k ? src[(b + l) * XS + tid] : 0.f;
-#pragma unroll
-      for (int l = 0; l < 8; ++l) {
-        if (b + l < k) {
-          x[l] *= rinv[b + l];
-#pragma unroll
-          for (int j = l + 1; j < 8; ++j) x[j] = fmaf(-x[l], Rc[(b + j) * RCS + b + l], x[j]);
-        }
-      }
-#pragma unroll
-      for (int l = 0; l < 8; ++l)
-        if (b + l < k) Y[(b + l) * XS + tid] = x[l];
-    }
-    const int nj = k - b - 8;
-    if (nj > 0) {
-      for (int e = tid; e < 8 * 32; e += LT) {
-        const int i = e / 32, j = e % 32;
-        Rt[i * RCS + j] = (j < nj) ? Rc[(b + 8 + j) * RCS + b + i] : 0.f;
-      }
-    }
-    __syncthreads();
-    if (nj > 0) {
-      if (b == 0)
-        slab_gemm_sub(Y, 8, X, a0 + 8, Y, 0, 8, Rt, RCS, nj, rows_eff);
-      else
-        slab_gemm_sub(Y, b + 8, Y, b + 8, Y, b, 8, Rt, RCS, nj, rows_eff);
-      __syncthreads();
     }
   }
 }
@@ -775,6 +725,61 @@ __device__ bool res_project_rest(const LeafPlan& P, ResSmem& S, GridSync& gs, in
 // first-pass Gram matrix is H - C_next^T C_next (the update removes exactly
 // the component along the orthonormal Q), so that panel skips its first
 // reduction (*h_out; its second CholQR pass runs on the data as always).
+// Named barriers of the pipelined first pass: warp 0 (the Cholesky) arrives on
+// kPubBar + g once pivot group g (eight pivots) is final, one id per group, so
+// an arrival can never fall into an earlier group's barrier; warps 1..7 sync
+// on it, and on kSolveBar (224 threads) between the phases of each block.
+constexpr int kSolveBar = 2, kPubBar = 3, kSolveThreads = LT - 32;  // ids 3 .. 6 for k <= 32
+
+// slab_solve run by warps 1..7 behind the Cholesky on warp 0: block b of
+// eight columns starts once pivots b .. b+7 are published.
+__device__ void slab_solve_behind(float* Y, const float* X, int a0, int k, int rows, int rows_eff, const float* Rc,
+                                  const float* rinv, float* Rt) {
+  const int ct = static_cast<int>(threadIdx.x) - 32;
+  for (int b = 0; b < k; b += 8) {
+    asm volatile("bar.sync %0, %1;" ::"r"(kPubBar + b / 8), "r"(LT) : "memory");
+    for (int r = ct; r < rows_eff; r += kSolveThreads) {
+      if (r >= rows) {
+        if (b == 0) {
+#pragma unroll
+          for (int l = 0; l < 8; ++l) Y[l * XS + r] = 0.f;
+        }
+        continue;
+      }
+      const float* src = b == 0 ? X + a0 * XS : Y;
+      float x[8];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) x[l] = b + l < k ? src[(b + l) * XS + r] : 0.f;
+#pragma unroll
+      for (int l = 0; l < 8; ++l) {
+        if (b + l < k) {
+          x[l] *= rinv[b + l];
+#pragma unroll
+          for (int j = l + 1; j < 8; ++j) x[j] = fmaf(-x[l], Rc[(b + j) * RCS + b + l], x[j]);
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < 8; ++l)
+        if (b + l < k) Y[(b + l) * XS + r] = x[l];
+    }
+    const int nj = k - b - 8;
+    if (nj > 0) {
+      for (int e = ct; e < 8 * 32; e += kSolveThreads) {
+        const int i = e / 32, j = e % 32;
+        Rt[i * RCS + j] = (j < nj) ? Rc[(b + 8 + j) * RCS + b + i] : 0.f;
+      }
+    }
+    asm volatile("bar.sync %0, %1;" ::"r"(kSolveBar), "r"(kSolveThreads) : "memory");
+    if (nj > 0) {
+      if (b == 0)
+        slab_gemm_sub(Y, 8, X, a0 + 8, Y, 0, 8, Rt, RCS, nj, rows_eff, ct, kSolveThreads);
+      else
+        slab_gemm_sub(Y, b + 8, Y, b + 8, Y, b, 8, Rt, RCS, nj, rows_eff, ct, kSolveThreads);
+      asm volatile("bar.sync %0, %1;" ::"r"(kSolveBar), "r"(kSolveThreads) : "memory");
+    }
+  }
+}
+
 __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, int c0, int k, int r0,
                           int rows, int rest0, int nrest, bool h_in, bool* h_out) {
   ResPanelSmem& ps = S.p;
@@ -804,13 +809,17 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
         [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
   }
   __syncthreads();
-  chol_upper(ps.G, k, ps.R1, ps.rinv1, false, &ps.ok);
+  // ---- Cholesky on warp 0; Y = X R1^-1 (rows of the slab) on warps 1..7 behind it,
+  // block by block (Y is scratch: a failed factorisation leaves X untouched)
+  if (tid < 32)
+    chol_upper(ps.G, k, ps.R1, ps.rinv1, false, &ps.ok, 1e-4f, kPubBar);
+  else
+    slab_solve_behind(S.Y, S.X, c0, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2);
   __syncthreads();
   if (!ps.ok)
     return res_fallback(P, S, gs, okflag, c0, k, r0, rows) &&
            res_project_rest(P, S, gs, okflag, c0, k, rest0, nrest, rows);
-  // ---- Y = X R1^-1 (rows of the slab), G2 = Y^T Y (and P = Y^T A_rest)
-  slab_solve(S.Y, S.X, c0, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2);
+  // ---- G2 = Y^T Y (and P = Y^T A_rest)
   if (tid == 0) ps.devbits = 0;
   if (nrest == 0) {
     res_tn(S.Y, 0, k, S.Y, 0, k, rows_eff, S.gp, P.part);
@@ -834,17 +843,25 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
     if (!grid_barrier(gs, okflag)) return false;
     reduce_partials(P.part, 32, 32 + nrest + kn, 32, [&](int e, float v) { P.red[e] = v; });
     if (!grid_barrier(gs, okflag)) return false;
-    const int nh = 1024 + 32 * nrest;
-    batched_copy(
-        nh + 32 * kn, [&](int e) { return __ldcg(&P.red[e]); },
-        [&](int e, float v) {
-          if (e < 1024)
-            ps.G[(e % 32) * 33 + e / 32] = v;
-          else if (e < nh)
-            S.Pm[(e % 32) * PMS + (e - 1024) / 32] = v;
-          else
-            S.Hn[(e % 32) * 33 + (e - nh) / 32] = v;
-        });
+    // all of a thread's loads in flight at once (at most 20: 32 x 160 entries / 256 threads)
+    const int nh = 1024 + 32 * nrest, ntot = nh + 32 * kn;
+    constexpr int kCp = (32 * 160 + LT - 1) / LT;
+    float cv[kCp];
+#pragma unroll
+    for (int u = 0; u < kCp; ++u) {
+      const int e = tid + u * LT;
+      cv[u] = e < ntot ? __ldcg(&P.red[e]) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < kCp; ++u) {
+      const int e = tid + u * LT;  // e % 32 == tid % 32 for every u
+      if (e < 1024)
+        ps.G[(e % 32) * 33 + e / 32] = cv[u];
+      else if (e < nh)
+        S.Pm[(e % 32) * PMS + (e - 1024) / 32] = cv[u];
+      else if (e < ntot)
+        S.Hn[(e % 32) * 33 + (e - nh) / 32] = cv[u];
+    }
   }
   __syncthreads();
   // G2 = I + E. When max |E| <= 3e-4, chol(I + E) = I + F + O(E^2) with
