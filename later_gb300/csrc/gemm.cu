@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
 #include <mutex>
 
 #include "ptx.cuh"
@@ -410,6 +411,290 @@ __global__ void __launch_bounds__(256) splitk_reduce_kernel(const GemmArgs p) {
   }
 }
 
+// ------------------------------------------------------- persistent kernel
+// One CTA per SM walks the output tiles t = blockIdx.x, + gridDim.x, ... (the
+// grouped order of tile_coords), without split-K. Warp 0 lane 0 issues the TMA
+// loads and warp 1 lane 0 the MMAs continuously across tiles: the stage ring's
+// index and phase follow one k-block counter over all of the CTA's tiles.
+// Accumulators: NACC TMEM buffers of ACC_COLS columns; the MMA of tile i goes
+// to buffer i % NACC once the epilogue has drained that buffer's previous use
+// (tmem_empty), and signals tmem_full when its MMAs complete. Warps 4..11 run
+// the epilogue (two warps per TMEM lane quarter, alternate 32-column chunks),
+// so with NACC = 2 the epilogue of one tile overlaps the mainloop of the next,
+// and the loads of the next tile overlap the epilogue in any case. Before
+// waiting for a tile they prefetch its C block into L2. Every wait is bounded;
+// on a timeout the CTA sets DEV_TIMEOUT, stops issuing, drains its loads and
+// MMAs, and returns.
+constexpr int kPersistThreads = 384;
+constexpr int kEpiWarp0 = 4;  // warps 4 .. 11
+constexpr int kEpiThreads = 256;
+
+template <int BN, bool A_MN, bool B_MN, int SPL, int STAGES, int NACC>
+struct PCfg {
+  using Base = Cfg<BN, A_MN, B_MN, SPL, STAGES>;
+  static_assert(Base::TMEM_COLS > 0 && Base::SMEM > 0, "stage layout shared with the one-tile kernel");
+  static constexpr int ACC_COLS = SPL ? 2 * BN : BN;
+  static constexpr int TMEM_COLS = NACC * ACC_COLS;
+  static constexpr int SMEM = STAGES * Base::STAGE_BYTES + 1024 + 256;
+};
+
+template <int BN, bool A_MN, bool B_MN, int SPL, int STAGES, int NACC>
+__global__ void __launch_bounds__(kPersistThreads, 1)
+    tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                              const __grid_constant__ CUtensorMap tmAl, const __grid_constant__ CUtensorMap tmBl,
+                              const GemmArgs p) {
+  using C_ = Cfg<BN, A_MN, B_MN, SPL, STAGES>;
+  using P_ = PCfg<BN, A_MN, B_MN, SPL, STAGES, NACC>;
+  static_assert(P_::TMEM_COLS == 32 || P_::TMEM_COLS == 64 || P_::TMEM_COLS == 128 || P_::TMEM_COLS == 256 ||
+                    P_::TMEM_COLS == 512,
+                "tmem allocation must be a power of two in [32, 512]");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * C_::STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;
+  uint64_t* tempty = tfull + NACC;
+  uint64_t* done = tempty + NACC;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int ntiles = p.tiles_m * p.tiles_n;
+  const int nkb = p.kb_total;
+  // Same skip rule in every role: a lower-triangular output's tiles entirely above the diagonal.
+  auto skip = [&](int t) {
+    int tm, tn;
+    tile_coords(t, p.tiles_m, p.tiles_n, &tm, &tn);
+    return p.lower && tm * BM + BM - 1 < tn * BN + p.diag;
+  };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < NACC; ++a) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], kEpiThreads);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, P_::TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ------------------------------------------------------- producer
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      if (SPL) tma_prefetch_desc(&tmAl);
+      if (SPL == 2) tma_prefetch_desc(&tmBl);
+      uint32_t g = 0;
+      for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+        if (skip(t)) continue;
+        int tm, tn;
+        tile_coords(t, p.tiles_m, p.tiles_n, &tm, &tn);
+        const int m0 = tm * BM, n0 = tn * BN;
+        for (int i = 0; i < nkb; ++i, ++g) {
+          const int s = g % STAGES;
+          const uint32_t ph = (g / STAGES) & 1;
+          if (g >= STAGES && !mbar_wait(&empty[s], ph ^ 1, p.budget)) {
+            *abort_flag = 1;
+            break;
+          }
+          if (*abort_flag) break;
+          uint8_t* sa = smem + s * C_::STAGE_BYTES;
+          uint8_t* sb = sa + C_::A_OPS * C_::A_BYTES;
+          const int k0 = i * BK;
+          mbar_arrive_expect_tx(&full[s], C_::STAGE_BYTES);
+#pragma unroll
+          for (int op = 0; op < C_::A_OPS; ++op) {
+            const CUtensorMap* ma = op ? &tmAl : &tmA;
+            uint8_t* da = sa + op * C_::A_BYTES;
+            if (A_MN) {
+              tma_load_2d(da, ma, &full[s], m0, k0);
+              tma_load_2d(da + BK * 128, ma, &full[s], m0 + 64, k0);
+            } else {
+              tma_load_2d(da, ma, &full[s], k0, m0);
+            }
+          }
+#pragma unroll
+          for (int op = 0; op < C_::B_OPS; ++op) {
+            const CUtensorMap* mb = op ? &tmBl : &tmB;
+            uint8_t* db = sb + op * C_::B_BYTES;
+            if (B_MN) {
+#pragma unroll
+              for (int c = 0; c < BN / 64; ++c) tma_load_2d(db + c * BK * 128, mb, &full[s], n0 + 64 * c, k0);
+            } else {
+              tma_load_2d(db, mb, &full[s], k0, n0);
+            }
+          }
+        }
+      }
+      // Drain: every issued load must land before the CTA may exit.
+      for (uint32_t j = (g > STAGES ? g - STAGES : 0); j < g; ++j)
+        mbar_wait(&full[j % STAGES], (j / STAGES) & 1, kDrainBudgetCycles);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ------------------------------------------------------- MMA issuer
+      const uint32_t idesc = idesc_f16(BM, BN, p.ab_bf16, A_MN ? 1 : 0, B_MN ? 1 : 0);
+      uint32_t g = 0;
+      int lt = 0;
+      for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+        if (skip(t)) continue;
+        const int a = lt % NACC, use = lt / NACC;
+        if (use > 0 && !mbar_wait(&tempty[a], (use - 1) & 1, p.budget)) {
+          *abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc_base = tmem + a * P_::ACC_COLS;
+        for (int i = 0; i < nkb; ++i, ++g) {
+          const int s = g % STAGES;
+          const uint32_t ph = (g / STAGES) & 1;
+          if (!mbar_wait(&full[s], ph, p.budget)) {
+            *abort_flag = 1;
+            break;
+          }
+          if (*abort_flag) break;
+          tc_fence_after();
+          const uint32_t sa = smem_u32(smem + s * C_::STAGE_BYTES);
+          const uint32_t sb = sa + C_::A_OPS * C_::A_BYTES;
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            const uint32_t a_off = A_MN ? k * 16 * 128 : k * 32;
+            const uint32_t b_off = B_MN ? k * 16 * 128 : k * 32;
+            const uint64_t ad = smem_desc_sw128(sa + a_off, A_MN ? BK * 128 : 16, 1024);
+            const uint64_t bd = smem_desc_sw128(sb + b_off, B_MN ? BK * 128 : 16, 1024);
+            const uint32_t acc = (i > 0 || k > 0) ? 1u : 0u;
+            tc_mma_f16(acc_base, ad, bd, idesc, acc);
+            if (SPL == 2) {
+              const uint64_t adl = smem_desc_sw128(sa + C_::A_BYTES + a_off, A_MN ? BK * 128 : 16, 1024);
+              const uint64_t bdl = smem_desc_sw128(sb + C_::B_BYTES + b_off, B_MN ? BK * 128 : 16, 1024);
+              tc_mma_f16(acc_base + BN, ad, bdl, idesc, acc);
+              tc_mma_f16(acc_base + BN, adl, bd, idesc, 1u);
+            } else if (SPL == 1) {
+              const uint64_t adl = smem_desc_sw128(sa + C_::A_BYTES + a_off, A_MN ? BK * 128 : 16, 1024);
+              tc_mma_f16(acc_base + BN, adl, bd, idesc, acc);
+            }
+          }
+          tc_commit(&empty[s]);
+        }
+        if (*abort_flag) break;
+        tc_commit(&tfull[a]);  // arrives once this tile's MMAs have completed
+        ++lt;
+      }
+      tc_commit(done);  // every MMA issued above has completed when this arrives
+      mbar_wait(done, 0, kDrainBudgetCycles);
+    }
+  } else if (warp >= kEpiWarp0) {
+    // ------------------------------------------------------- epilogue
+    const int ew = warp - kEpiWarp0;
+    const int quarter = warp & 3, half = ew >> 2;  // TMEM lanes 32 (warp % 4) .. + 31
+    const int r = quarter * 32 + lane;
+    int lt = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      if (skip(t)) continue;
+      int tm, tn;
+      tile_coords(t, p.tiles_m, p.tiles_n, &tm, &tn);
+      const int m0 = tm * BM, n0 = tn * BN;
+      // this tile's C block into L2 while its MMAs run
+      if (p.beta != 0.f) {
+        const int rows = min(BM, p.M - m0), ncols = min(BN, p.N - n0);
+        const int lines = (rows + 31) / 32;
+        for (int e = threadIdx.x - kEpiWarp0 * 32; e < ncols * lines; e += kEpiThreads) {
+          const int c = e / lines, l = e % lines;
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(p.C + m0 + 32 * l + static_cast<int64_t>(n0 + c) * p.ldc));
+        }
+      }
+      const int a = lt % NACC, use = lt / NACC;
+      if (!mbar_wait(&tfull[a], use & 1, p.budget)) {
+        if (threadIdx.x == kEpiWarp0 * 32) report(p.status, DEV_TIMEOUT);
+        *abort_flag = 1;
+        break;
+      }
+      tc_fence_after();
+      const int row = m0 + r;
+      const uint32_t t_row = tmem + a * P_::ACC_COLS + (static_cast<uint32_t>(quarter * 32) << 16);
+      const bool rd = (p.beta != 0.f) && row < p.M;
+      float cv[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int col = n0 + 32 * half + j;
+        cv[j] = (rd && 32 * half < BN && col < p.N) ? p.C[row + static_cast<int64_t>(col) * p.ldc] : 0.f;
+      }
+#pragma unroll 1
+      for (int c0 = 32 * half; c0 < BN; c0 += 64) {
+        float v[32];
+        tmem_ld_32x32b_x32(t_row + c0, v);
+        if (SPL) {
+          float w[32];
+          tmem_ld_32x32b_x32(t_row + BN + c0, w);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] += w[j] * kLoScaleInv;
+        }
+        float cn[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = n0 + c0 + 64 + j;
+          cn[j] = (rd && c0 + 64 < BN && col < p.N) ? p.C[row + static_cast<int64_t>(col) * p.ldc] : 0.f;
+        }
+        if (row < p.M && n0 + c0 + 32 <= p.N && !p.lower) {
+          epilogue_chunk(p, row, n0 + c0, v, cv);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) epilogue_store_c(p, row, n0 + c0 + j, v[j], cv[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) cv[j] = cn[j];
+      }
+      tc_fence_before();
+      mbar_arrive(&tempty[a]);  // this thread's reads of buffer a are complete
+      ++lt;
+    }
+  }
+  __syncwarp();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) tmem_dealloc(tmem, P_::TMEM_COLS);
+}
+
+template <int BN, bool A_MN, bool B_MN, int SPL, int STAGES, int NACC>
+later_status_t launch_persistent(const CUtensorMap& a, const CUtensorMap& b, const CUtensorMap& al,
+                                 const CUtensorMap& bl, const GemmArgs& args, int ctas, cudaStream_t st) {
+  using P_ = PCfg<BN, A_MN, B_MN, SPL, STAGES, NACC>;
+  static_assert(P_::SMEM <= 227 * 1024, "shared memory");
+  auto kern = tc_gemm_persistent_kernel<BN, A_MN, B_MN, SPL, STAGES, NACC>;
+  static bool attr_done[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr_done[dev]) {
+    LATER_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P_::SMEM));
+    attr_done[dev] = true;
+  }
+  kern<<<ctas, kPersistThreads, P_::SMEM, st>>>(a, b, al, bl, args);
+  note_launch();
+  LATER_CHECK_CUDA(cudaGetLastError());
+  return LATER_OK;
+}
+
+// The trailing-update shapes of rgsqrf: TN (R12 = Q1^T A2) and NN (A2 -= Q1 R12).
+template <int BN, int SPL, int STAGES, int NACC>
+later_status_t launch_persistent_ab(bool a_mn, bool b_mn, const CUtensorMap& a, const CUtensorMap& b,
+                                    const CUtensorMap& al, const CUtensorMap& bl, const GemmArgs& args, int ctas,
+                                    cudaStream_t st) {
+  if (b_mn) return LATER_ERR_NOT_SUPPORTED;
+  if (a_mn) return launch_persistent<BN, true, false, SPL, STAGES, NACC>(a, b, al, bl, args, ctas, st);
+  return launch_persistent<BN, false, false, SPL, STAGES, NACC>(a, b, al, bl, args, ctas, st);
+}
+
 // ------------------------------------------------------------------- host
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -476,6 +761,15 @@ bool make_map16(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols
                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
+}
+
+// The persistent kernel is used unless LATER_GEMM_PERSISTENT=0 (kept for A/B timing).
+bool persistent_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("LATER_GEMM_PERSISTENT");
+    return !(e && e[0] == '0');
+  }();
+  return on;
 }
 
 later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, long long budget) {
@@ -563,6 +857,20 @@ later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, lon
 
   dim3 grid(tiles, splits);
   TraceScope trace(st, TRACE_GEMM, 2.0 * g.M * g.N * static_cast<double>(g.K));
+  if (splits == 1 && !b_mn && persistent_enabled()) {
+    const int ctas = tiles < nsm ? tiles : nsm;
+    later_status_t r = LATER_ERR_NOT_SUPPORTED;
+    if (split3) {
+      if (BN == 128) r = launch_persistent_ab<128, 2, 3, 2>(a_mn, b_mn, ma, mb, mal, mbl, a, ctas, st);
+    } else if (split_a) {
+      if (BN == 256) r = launch_persistent_ab<256, 1, 3, 1>(a_mn, b_mn, ma, mb, mal, mbl, a, ctas, st);
+      else if (BN == 128) r = launch_persistent_ab<128, 1, 4, 2>(a_mn, b_mn, ma, mb, mal, mbl, a, ctas, st);
+    } else {
+      if (BN == 256) r = launch_persistent_ab<256, 0, 4, 2>(a_mn, b_mn, ma, mb, mal, mbl, a, ctas, st);
+      else if (BN == 128) r = launch_persistent_ab<128, 0, 6, 2>(a_mn, b_mn, ma, mb, mal, mbl, a, ctas, st);
+    }
+    if (r != LATER_ERR_NOT_SUPPORTED) return r;
+  }
   if (split3) {
     if (BN == 64) return launch_bn<64, 2, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
     return launch_bn<128, 2, 3>(a_mn, b_mn, ma, mb, mal, mbl, a, grid, st);
