@@ -589,7 +589,8 @@ def run_serve(a):
     for A, B in pool[:8]:
         srv.wait(srv.submit(A, B))
     serial = (time.perf_counter() - t0) / 8
-    rates = a.rates or [0.5 / serial, 1.0 / serial, 2.0 / serial, 4.0 / serial]
+    # from half the serial rate up to well past saturation (the top rates measure capacity)
+    rates = a.rates or [f / serial for f in (0.5, 1.0, 2.0, 4.0, 8.0, 16.0)]
     results = []
     for lam in rates:
         arr = np.cumsum(rng.exponential(1.0 / lam, a.requests))
