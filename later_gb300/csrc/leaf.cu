@@ -600,12 +600,15 @@ __device__ void res_store(const LeafPlan& P, const float* X, int r0, int rows, i
 // groups' sums are added in group order.
 // Optional second B buffer: B's columns c >= nb1 are columns b20 + c - nb1 of
 // Xb2 (so [Y | X_rest] is one operand); nb up to 128 (at most 256 4x4 tiles).
+// Run by threads [t0, t0 + nthr) of the CTA; bar >= 0 names the barrier those
+// threads share (else the whole CTA runs it and __syncthreads is used).
 template <class Emit>
 __device__ void res_tn_emit(const float* Xa, int a0, int na, const float* Xb, int b0, int nb, int rows_eff,
-                            float* gp, Emit emit, const float* Xb2 = nullptr, int b20 = 0, int nb1 = 1 << 30) {
-  const int tid = threadIdx.x;
+                            float* gp, Emit emit, const float* Xb2 = nullptr, int b20 = 0, int nb1 = 1 << 30,
+                            int t0 = 0, int nthr = LT, int bar = -1) {
+  const int tid = static_cast<int>(threadIdx.x) - t0;
   const int nta = (na + 3) / 4, ntb = (nb + 3) / 4, nt = nta * ntb;
-  const int groups = max(1, LT / nt);
+  const int groups = max(1, nthr / nt);
   const int g = tid / nt, t = tid % nt;
   const int ti = t % nta, tj = t / nta;
   const int npad = 16 * nt;
@@ -640,8 +643,11 @@ __device__ void res_tn_emit(const float* Xa, int a0, int na, const float* Xb, in
 #pragma unroll
       for (int v = 0; v < 4; ++v) gp[g * npad + (ti + nta * u) + 4 * nta * (tj + ntb * v)] = acc[u][v];
   }
-  __syncthreads();
-  for (int e = tid; e < npad; e += LT) {
+  if (bar < 0)
+    __syncthreads();
+  else
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthr) : "memory");
+  for (int e = tid; e < npad; e += nthr) {
     float s = 0.f;
     for (int gg = 0; gg < groups; ++gg) s += gp[gg * npad + e];
     emit(e % (4 * nta), e / (4 * nta), s);
@@ -733,9 +739,17 @@ constexpr int kSolveBar = 2, kPubBar = 3, kSolveThreads = LT - 32;  // ids 3 .. 
 
 // slab_solve run by warps 1..7 behind the Cholesky on warp 0: block b of
 // eight columns starts once pivots b .. b+7 are published.
+// First, while the first pivots are computed, the partial Gram matrix of the
+// next panel's columns [hn0, hn0 + kn) (kn > 0) goes to hpart[i + 32 j].
 __device__ void slab_solve_behind(float* Y, const float* X, int a0, int k, int rows, int rows_eff, const float* Rc,
-                                  const float* rinv, float* Rt) {
+                                  const float* rinv, float* Rt, float* gp, int hn0, int kn, float* hpart) {
   const int ct = static_cast<int>(threadIdx.x) - 32;
+  if (kn > 0) {
+    res_tn_emit(
+        X, hn0, kn, X, hn0, kn, rows_eff, gp, [&](int i, int j, float v) { hpart[i + 32 * j] = v; }, nullptr, 0,
+        1 << 30, 32, kSolveThreads, kSolveBar);
+    asm volatile("bar.sync %0, %1;" ::"r"(kSolveBar), "r"(kSolveThreads) : "memory");  // gp reused later
+  }
   for (int b = 0; b < k; b += 8) {
     asm volatile("bar.sync %0, %1;" ::"r"(kPubBar + b / 8), "r"(LT) : "memory");
     for (int r = ct; r < rows_eff; r += kSolveThreads) {
@@ -811,10 +825,14 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
   __syncthreads();
   // ---- Cholesky on warp 0; Y = X R1^-1 (rows of the slab) on warps 1..7 behind it,
   // block by block (Y is scratch: a failed factorisation leaves X untouched)
+  // (warps 1..7 first compute the next panel's Gram partial, H, in the wait for the first pivots)
+  const int kn_next = min(32, nrest);
+  float* prt = P.part + static_cast<int64_t>(blockIdx.x) * PART;
   if (tid < 32)
     chol_upper(ps.G, k, ps.R1, ps.rinv1, false, &ps.ok, 1e-4f, kPubBar);
   else
-    slab_solve_behind(S.Y, S.X, c0, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2);
+    slab_solve_behind(S.Y, S.X, c0, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2, S.gp, rest0, kn_next,
+                      prt + 32 * (32 + nrest));
   __syncthreads();
   if (!ps.ok)
     return res_fallback(P, S, gs, okflag, c0, k, r0, rows) &&
@@ -831,15 +849,15 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
         [&](int e, float v) { ps.G[(e % 32) * 33 + e / 32] = v; });
   } else {
     // partial of [Y^T Y | Y^T A_rest], entry (i, j) at i + 32 j (k = 32)
-    // partial of [Y^T Y | Y^T A_rest | A_next^T A_next], entry (i, j) at i + 32 j (k = 32)
-    const int kn = min(32, nrest);
-    float* prt = P.part + static_cast<int64_t>(blockIdx.x) * PART;
+    // partial of [Y^T Y | Y^T A_rest | A_next^T A_next], entry (i, j) at i + 32 j (k = 32);
+    // the A_next^T A_next block was written during the Cholesky
+    const int kn = kn_next;
     res_tn_emit(
-        S.Y, 0, 32, S.Y, 0, 32 + nrest, rows_eff, S.gp, [&](int i, int j, float v) { prt[i + 32 * j] = v; }, S.X,
-        rest0, 32);
-    __syncthreads();  // gp is reused
-    res_tn_emit(S.X, rest0, kn, S.X, rest0, kn, rows_eff, S.gp,
-                [&](int i, int j, float v) { prt[i + 32 * (32 + nrest + j)] = v; });
+        S.Y, 0, 32, S.Y, 0, 32 + nrest, rows_eff, S.gp,
+        [&](int i, int j, float v) {
+          if (j < 32 + nrest) prt[i + 32 * j] = v;  // padded columns would overwrite the H block
+        },
+        S.X, rest0, 32);
     if (!grid_barrier(gs, okflag)) return false;
     reduce_partials(P.part, 32, 32 + nrest + kn, 32, [&](int e, float v) { P.red[e] = v; });
     if (!grid_barrier(gs, okflag)) return false;

@@ -96,7 +96,7 @@ def test_rgsqrf_rejects_bad_args(cuda):
         lg.later_rgsqrf(A)  # m < n
 
 
-@pytest.mark.parametrize("m,n", [(1000, 100), (700, 17), (4096, 333)])
+@pytest.mark.parametrize("m,n", [(1000, 100), (700, 17), (4096, 333), (2000, 127)])
 def test_rgsqrf_any_width(cuda, m, n):
     A = gen.normal(m, n, seed=n)
     Q, R = run_gpu(A)
