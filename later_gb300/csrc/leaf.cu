@@ -802,16 +802,27 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
   *h_out = false;
   // ---- G = A^T A
   if (h_in) {
-    // H - C^T C with C the previous panel's projection block of these columns (rows of Pm)
-    for (int e = tid; e < 1024; e += LT) {
-      const int i = e % 32, j = e / 32;
-      float v = 0.f;
-      if (i < k && j < k) {
-        v = S.Hn[i * 33 + j];
+    // H - C^T C with C the previous panel's projection block of these columns (rows of Pm):
+    // one 2 x 2 tile per thread, float2 reads of C's rows
+    {
+      const int ti = tid % 16, tj = tid / 16;
+      float acc[2][2] = {};
 #pragma unroll 8
-        for (int l = 0; l < 32; ++l) v = fmaf(-S.Pm[l * PMS + i], S.Pm[l * PMS + j], v);
+      for (int l = 0; l < 32; ++l) {
+        const float2 a = *reinterpret_cast<const float2*>(&S.Pm[l * PMS + 2 * ti]);
+        const float2 b = *reinterpret_cast<const float2*>(&S.Pm[l * PMS + 2 * tj]);
+        acc[0][0] = fmaf(a.x, b.x, acc[0][0]);
+        acc[0][1] = fmaf(a.x, b.y, acc[0][1]);
+        acc[1][0] = fmaf(a.y, b.x, acc[1][0]);
+        acc[1][1] = fmaf(a.y, b.y, acc[1][1]);
       }
-      ps.G[i * 33 + j] = v;
+#pragma unroll
+      for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const int i = 2 * ti + u, j = 2 * tj + v;
+          ps.G[i * 33 + j] = (i < k && j < k) ? S.Hn[i * 33 + j] - acc[u][v] : 0.f;
+        }
     }
   } else {
     res_tn(S.X, c0, k, S.X, c0, k, rows_eff, S.gp, P.part);
@@ -870,24 +881,32 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
       const int e = tid + u * LT;
       cv[u] = e < ntot ? __ldcg(&P.red[e]) : 0.f;
     }
+    float dev = 0.f;  // max |G2 - I| (k = 32 here; a NaN counts as a large deviation)
 #pragma unroll
     for (int u = 0; u < kCp; ++u) {
       const int e = tid + u * LT;  // e % 32 == tid % 32 for every u
-      if (e < 1024)
+      if (e < 1024) {
         ps.G[(e % 32) * 33 + e / 32] = cv[u];
-      else if (e < nh)
+        const float d = fabsf(cv[u] - ((e % 32) == (e / 32) ? 1.f : 0.f));
+        dev = d <= dev ? dev : (d == d ? d : 1.f);
+      } else if (e < nh) {
         S.Pm[(e % 32) * PMS + (e - 1024) / 32] = cv[u];
-      else if (e < ntot)
+      } else if (e < ntot) {
         S.Hn[(e % 32) * 33 + (e - nh) / 32] = cv[u];
+      }
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dev = fmaxf(dev, __shfl_xor_sync(0xffffffffu, dev, o));
+    if ((tid & 31) == 0) atomicMax(&ps.devbits, __float_as_int(dev));
   }
   __syncthreads();
   // G2 = I + E. When max |E| <= 3e-4, chol(I + E) = I + F + O(E^2) with
   // F = triu(E) - diag(E) / 2, and Q = Y (I - F) has Q^T Q = I + O(E^2) and
   // Q (I + F) R1 = Y R1 + O(E^2): no second Cholesky and no second
   // substitution chain, only a small product. Otherwise the exact path.
-  // max |E| over all threads (a NaN entry counts as a large deviation).
-  {
+  // max |E| over all threads (a NaN entry counts as a large deviation); the
+  // fused path took it while copying G2.
+  if (nrest == 0) {
     float dev = 0.f;
     for (int e = tid; e < 1024; e += LT) {
       const int i = e / 32, j = e % 32;
