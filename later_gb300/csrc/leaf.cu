@@ -739,11 +739,19 @@ constexpr int kSolveBar = 2, kPubBar = 3, kSolveThreads = LT - 32;  // ids 3 .. 
 
 // slab_solve run by warps 1..7 behind the Cholesky on warp 0: block b of
 // eight columns starts once pivots b .. b+7 are published.
-// First, while the first pivots are computed, the partial Gram matrix of the
-// next panel's columns [hn0, hn0 + kn) (kn > 0) goes to hpart[i + 32 j].
-__device__ void slab_solve_behind(float* Y, const float* X, int a0, int k, int rows, int rows_eff, const float* Rc,
-                                  const float* rinv, float* Rt, float* gp, int hn0, int kn, float* hpart) {
+// First, while the first pivots are computed: the previous panel's deferred
+// update of this panel and the later columns, X[:, a0 .. a0 + nsub) -= Q_prev
+// C_prev (nsub > 0; Q_prev = the 32 columns before a0, C_prev row-major in
+// Cprev), then the partial Gram matrix of the next panel's columns
+// [hn0, hn0 + kn) (kn > 0) into hpart[i + 32 j].
+__device__ void slab_solve_behind(float* Y, float* X, int a0, int k, int rows, int rows_eff, const float* Rc,
+                                  const float* rinv, float* Rt, float* gp, int hn0, int kn, float* hpart, int nsub,
+                                  const float* Cprev) {
   const int ct = static_cast<int>(threadIdx.x) - 32;
+  if (nsub > 0) {
+    slab_gemm_sub(X, a0, X, a0, X, a0 - 32, 32, Cprev, PMS, nsub, rows_eff, ct, kSolveThreads);
+    asm volatile("bar.sync %0, %1;" ::"r"(kSolveBar), "r"(kSolveThreads) : "memory");
+  }
   if (kn > 0) {
     res_tn_emit(
         X, hn0, kn, X, hn0, kn, rows_eff, gp, [&](int i, int j, float v) { hpart[i + 32 * j] = v; }, nullptr, 0,
@@ -839,11 +847,12 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
   // (warps 1..7 first compute the next panel's Gram partial, H, in the wait for the first pivots)
   const int kn_next = min(32, nrest);
   float* prt = P.part + static_cast<int64_t>(blockIdx.x) * PART;
+  // (h_in: the previous panel left its update of these columns, C_prev in Pm, to this phase)
   if (tid < 32)
     chol_upper(ps.G, k, ps.R1, ps.rinv1, false, &ps.ok, 1e-4f, kPubBar);
   else
     slab_solve_behind(S.Y, S.X, c0, k, rows, rows_eff, ps.R1, ps.rinv1, ps.R2, S.gp, rest0, kn_next,
-                      prt + 32 * (32 + nrest));
+                      prt + 32 * (32 + nrest), h_in ? k + nrest : 0, S.Pm);
   __syncthreads();
   if (!ps.ok)
     return res_fallback(P, S, gs, okflag, c0, k, r0, rows) &&
@@ -994,8 +1003,8 @@ __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okfl
     }
     __syncthreads();
     const int n = 32 * nrest;
-    // A_rest -= Q C; R[panel, rest] = C (spread over the CTAs)
-    slab_gemm_sub(S.X, rest0, S.X, rest0, S.X, c0, 32, S.Pm, PMS, nrest, rows_eff);
+    // R[panel, rest] = C (spread over the CTAs); A_rest -= Q C is left to the next
+    // panel's Cholesky phase (warps 1..7), which reads C from Pm
     for (int e = static_cast<int>(blockIdx.x) * LT + tid; e < n; e += static_cast<int>(gridDim.x) * LT)
       P.R[(c0 + e % 32) + static_cast<int64_t>(rest0 + e / 32) * P.ldr] = S.Pm[(e % 32) * PMS + e / 32];
     *h_out = true;
