@@ -180,7 +180,7 @@ def run_reference(a, rank, world):
               f"GEMM operands) on {a.cpu_m}x{a.cpu_n}, N(0,1) seed {a.seed}")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": qr_flops(a.cpu_m, a.cpu_n) / v / 1e9,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": a.precision,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp16",
             "data": "synthetic", "config": workload_config(a),
             "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": ncores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
