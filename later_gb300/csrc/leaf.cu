@@ -10,16 +10,24 @@
 //
 //   panel (c0, k <= 32), CholQR2:
 //     G  = A^T A            slab partials -> barrier -> distributed reduction -> barrier
-//     R1 = chol(G)          every CTA, redundantly (bitwise identical)
-//     Q1 = A R1^-1          row-wise substitution, into scratch; G2 = Q1^T Q1 partials
-//     R2 = chol(G2)         (after the same reduction)
-//     Q  = Q1 R2^-1, R = R2 R1
+//                           (panels after the first: G = H - C^T C from the previous
+//                           panel's reduction, no reduction of their own)
+//     R1 = chol(G)          every CTA, redundantly (bitwise identical), on warp 0
+//     Y  = A R1^-1          row-wise substitution on warps 1..7, eight columns behind
+//                           the Cholesky (named barrier per group of eight pivots)
+//     G2 = Y^T Y            partials -> reduction, together with P = Y^T A_rest
+//                           (the later columns) and H = A_next^T A_next
+//     R2 = I + F (first order, max|G2 - I| <= 3e-4) or chol(G2); Q = Y R2^-1, R = R2 R1
+//     C  = Q^T A_rest       from P locally; R[panel, rest] = C; A_rest -= Q C is applied
+//                           by warps 1..7 during the next panel's Cholesky
 //   The panel falls back to MGS-TSQR (the reference's algorithm, the tree of
-//   tsqr_dev.cuh run over virtual blocks) when chol(G) meets a non-positive
-//   pivot or max|G2 - I| > 1/4; every CTA takes the same decision from the
-//   same numbers, and A is not written before it.
-//   update (Q cols [c0, c0+w1), A2 cols [c1, c1+w2)):
-//     P = Q^T A2 (partials -> reduction, also written into R), A2 -= Q P.
+//   tsqr_dev.cuh run over virtual blocks) when chol(G) meets a pivot below
+//   1e-4 of its column's squared norm or max|G2 - I| > 1/4; every CTA takes
+//   the same decision from the same numbers, and A is not written before it.
+//   Its later columns are then projected by separate update steps.
+//   With CGS2 the panels keep the recursive order of the reference, glued by
+//   update steps (Q cols [c0, c0+w1), A2 cols [c1, c1+w2)):
+//     P = Q^T A2 (partials -> reduction, also written into R), A2 -= Q P, twice.
 //
 // Determinism: the row slabs depend only on m and the grid size; every
 // reduction sums the per-CTA partials in CTA order (lane-strided, then a fixed
@@ -721,16 +729,6 @@ __device__ bool res_project_rest(const LeafPlan& P, ResSmem& S, GridSync& gs, in
   return true;
 }
 
-// One 32-column panel by CholQR2 (first-order second pass when G2 is within
-// 3e-4 of I). With nrest > 0 (right-looking steps, full 32-column panel), the
-// second reduction also carries P = Y^T A_rest for the leaf's later columns
-// [rest0, rest0 + nrest) and H = A_next^T A_next for the next panel's columns
-// (the first kn of them, before this panel's update): the projection C =
-// Q^T A_rest follows locally, C = (I - F)^T P (first order) or R2^-T P
-// (exact), then A_rest -= Q C and R[panel, rest] = C; and the next panel's
-// first-pass Gram matrix is H - C_next^T C_next (the update removes exactly
-// the component along the orthonormal Q), so that panel skips its first
-// reduction (*h_out; its second CholQR pass runs on the data as always).
 // Named barriers of the pipelined first pass: warp 0 (the Cholesky) arrives on
 // kPubBar + g once pivot group g (eight pivots) is final, one id per group, so
 // an arrival can never fall into an earlier group's barrier; warps 1..7 sync
@@ -802,6 +800,18 @@ __device__ void slab_solve_behind(float* Y, float* X, int a0, int k, int rows, i
   }
 }
 
+// One 32-column panel by CholQR2 (first-order second pass when G2 is within
+// 3e-4 of I). With nrest > 0 (right-looking steps, full 32-column panel), the
+// second reduction also carries P = Y^T A_rest for the leaf's later columns
+// [rest0, rest0 + nrest) and H = A_next^T A_next for the next panel's columns
+// (the first kn of them, before this panel's update): the projection C =
+// Q^T A_rest follows locally, C = (I - F)^T P (first order) or R2^-T P
+// (exact), and R[panel, rest] = C. The update A_rest -= Q C is left in Pm for
+// the next panel, whose warps 1..7 apply it during its Cholesky (h_in); that
+// panel's first-pass Gram matrix is H - C_next^T C_next (the update removes
+// exactly the component along the orthonormal Q), so it skips its first
+// reduction (*h_out; its second CholQR pass runs on the data as always).
+// After a fallback the update is applied at once and *h_out stays false.
 __device__ bool res_panel(const LeafPlan& P, ResSmem& S, GridSync& gs, int* okflag, int c0, int k, int r0,
                           int rows, int rest0, int nrest, bool h_in, bool* h_out) {
   ResPanelSmem& ps = S.p;

@@ -21,8 +21,10 @@ int64_t leaf_fused_work(int m);
 // Each 32-column panel is factored by CholQR2 (Gram, Cholesky, triangular
 // solve, twice); a panel whose Cholesky breaks down or whose second Gram
 // matrix is far from the identity is factored by MGS-TSQR instead, inside the
-// same launch. Panels are glued by block Gram-Schmidt updates in the order of
-// the recursive split (one more projection pass with cgs2). `sync` points to
+// same launch. Panels are right-looking: each projects all later columns of
+// the leaf in its second reduction (block MGS order). With cgs2 they are glued
+// by block Gram-Schmidt updates in the order of the recursive split, each
+// applied twice. `sync` points to
 // kLeafSyncInts zeroed ints; `tsqr_counters` to zeroed TSQR tree counters.
 // Returns LATER_ERR_NOT_SUPPORTED when the device cannot run the cooperative
 // launch (the caller then uses the multi-launch leaf).
