@@ -11,15 +11,25 @@
 // when asked, its 16-bit copy in the same pass, so the next GEMM of the
 // recursion reads its operand without a conversion pass.
 //
-// Structure (one CTA = one 128 x BN output tile, or one K-slice of it):
+// Two kernels share the stage layout and MMA issue:
+// tc_gemm_kernel (one CTA = one 128 x BN output tile, or one K-slice of it):
 //   warp 0 / lane 0 : TMA producer, STAGES-deep ring of 64-wide K blocks
 //   warp 1 / lane 0 : MMA issuer (tcgen05.mma, M=128, N=BN, K=16 steps);
 //                     warp 1 also owns the TMEM allocation
-//   warps 0-3       : epilogue, one TMEM lane quarter (32 rows) per warp
-// Split-K: CTAs of one tile write FP32 partial tiles; the last one to finish
-// (atomic ticket) sums them in split order, so results are deterministic.
+//   warps 2-7       : prefetch the tile's C block into L2 during the mainloop
+//   warps 0-7       : epilogue, two warps per TMEM lane quarter (32 rows),
+//                     alternate 32-column chunks
+//   Split-K: CTAs of one tile write FP32 partial tiles; splitk_reduce_kernel
+//   sums them in split order in a fixed tree, so results are deterministic.
+// tc_gemm_persistent_kernel (the TN / NN trailing updates without split-K):
+//   one CTA per SM walks the tiles; producer and MMA issuer run across tiles,
+//   two TMEM accumulators let warps 4-11 run one tile's epilogue while the next
+//   tile's MMAs run.
+// Tiles are visited in groups of 16 tile rows, so concurrent CTAs share A and
+// B panels through L2.
 // SPLIT3: A = Ah + Al/2048, B = Bh + Bl/2048 (FP16); three products go to two
-// TMEM accumulators, D = acc0 + acc1/2048.
+// TMEM accumulators, D = acc0 + acc1/2048. SPLIT2: A = Ah + Al/2048, B = Bh;
+// two products (Ah.Bh and Al.Bh) into two accumulators, combined the same way.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
