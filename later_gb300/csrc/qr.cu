@@ -10,7 +10,12 @@
 //   * R12 = Q1^T A2 splits K over idle SMs with a deterministic reduction;
 //   * the caller's lda is honoured (the reference passes m, :70);
 //   * R is written in full, zeros below the diagonal;
-//   * optional CGS2 (second projection pass) and SPLIT3 / BF16 precisions.
+//   * optional CGS2 (second projection pass) and SPLIT3 / BF16 precisions;
+//   * SPLIT2: R12 is one FP16 product stored at its FP16 value and A2 -= Q1 R12
+//     splits Q1 into hi + lo, so the factor subtracted is the factor stored
+//     (backward error at the FP32 level for 1.5x the FP16 tensor work);
+//   * each leaf is one cooperative launch (leaf.cu) unless the caller asks for
+//     the reference's MGS-TSQR panels.
 #include <cuda_runtime.h>
 
 #include <algorithm>
