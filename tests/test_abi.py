@@ -35,3 +35,21 @@ def test_bufsize_query_cpu():
     assert lh >= 4096 * 1024
     # The reference test's own work size (test/test_qr.cu:69) is enough to run.
     assert lw > 0
+
+
+def test_split2_workspace_holds_the_lo_copy():
+    # SPLIT2 keeps Q's lo copy for the A2 -= Q1 R12 update: the same 16-bit workspace as SPLIT3,
+    # twice the FP16 one.
+    _, h16 = lg.rgsqrf_bufsize(4096, 1024, precision="fp16")
+    _, h2 = lg.rgsqrf_bufsize(4096, 1024, precision="split2")
+    _, h3 = lg.rgsqrf_bufsize(4096, 1024, precision="split3")
+    assert h2 == h3 == 2 * h16
+
+
+def test_split2_is_rejected_outside_rgsqrf():
+    import pytest
+    # SPLIT2 is a trailing-update mode of the QR recursion; the BLAS3 / Cholesky routines refuse it.
+    for op in ("s", "t", "m", "p"):
+        with pytest.raises(lg.LaterError):
+            lg.blas3_bufsize(op, 512, 512, precision="split2")
+    lg.blas3_bufsize("p", 512, 512, precision="split3")  # the other modes stay valid
