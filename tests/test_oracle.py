@@ -88,3 +88,52 @@ def test_reference_literal_reconstruction_same_product():
     Qs, Qi = lo.ormqr(Ws, Ys), lo.ormqr(Wi, Yi)
     assert np.allclose(Qs @ np.triu(Rs), Qi @ np.triu(Ri), atol=1e-4)
     assert np.allclose(np.abs(np.triu(Rs)), np.abs(np.triu(Ri)), atol=1e-3)
+
+
+# Known answers on the reference tests' constant inputs (T = lower triangle of 0.1,
+# test/test_trsm.cu:44-56, test/test_trmm.cu:43-55, test/test_potrf.cu:38-62): the BLAS-3 and
+# Cholesky restatements are pinned to exact results, through their recursion (small leaves).
+def _T(n):
+    return gen.lower_tri_const(n)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp16", 6e-4), ("split3", 2e-6)])
+def test_rtrmm_oracle_known_answer(prec, tol):
+    n = 512
+    C = lo.rtrmm(_T(n), np.ones((n, 48), np.float32), prec=prec, leaf=64)
+    exact = np.repeat(0.1 * np.arange(1, n + 1, dtype=np.float64)[:, None], 48, axis=1)
+    assert np.abs(C - exact).max() / np.abs(exact).max() < tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp16", 1e-3), ("split3", 2e-6)])
+def test_rsyrk_oracle_known_answer(prec, tol):
+    n = 384
+    C = lo.rsyrk(1.0, _T(n), 0.0, np.zeros((n, n), np.float32), prec=prec)
+    i = np.arange(n)
+    exact = 0.01 * (np.minimum.outer(i, i) + 1)
+    il = np.tril_indices(n)
+    assert np.abs(C[il] - exact[il]).max() / exact.max() < tol
+    assert np.all(np.triu(C, 1) == 0)  # the upper triangle is not touched
+
+
+@pytest.mark.parametrize("side", ["l", "r"])
+def test_rtrsm_oracle_known_answer(side):
+    n, k = 512, 40
+    T = _T(n).astype(np.float64)
+    B = (T @ np.ones((n, k))) if side == "l" else (np.ones((k, n)) @ T.T)
+    B = B.astype(np.float32)
+    X3 = lo.rtrsm(side, _T(n), B, prec="split3", leaf=64)
+    assert np.abs(X3 - 1.0).max() < 1e-3  # the exact answer is all ones
+    X16 = lo.rtrsm(side, _T(n), B, prec="fp16", leaf=64).astype(np.float64)
+    res = (T @ X16 - B) if side == "l" else (X16 @ T.T - B)
+    assert np.linalg.norm(res) / np.linalg.norm(B) < 1e-3
+
+
+def test_rpotrf_oracle_known_answer():
+    n = 512
+    T = _T(n).astype(np.float64)
+    A = (T @ T.T).astype(np.float32)
+    L3 = lo.rpotrf(A, prec="split3", leaf=128).astype(np.float64)
+    assert np.linalg.norm(L3 - T) / np.linalg.norm(T) < 1e-3  # the factor of T T^T is T
+    L16 = lo.rpotrf(A, prec="fp16", leaf=128).astype(np.float64)
+    assert metrics.chol_backward_error(A, L16) < 1e-3
