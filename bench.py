@@ -64,6 +64,9 @@ def parse():
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    p.add_argument("--no-ref", action="store_true", help="skip the same-GPU reference / cuSOLVER comparators")
+    p.add_argument("--no-extras", action="store_true",
+                   help="qr: skip the C3 / C4 / C5 configurations that follow the headline in the same line")
     p.add_argument("--cpu-m", type=int, default=16384, help="CPU sample rows")
     p.add_argument("--cpu-n", type=int, default=1024, help="CPU sample columns")
     p.add_argument("--config", default="qr", choices=["qr", "spd", "batched", "serve"],
@@ -71,8 +74,9 @@ def parse():
                         "batched: 4096 uneven tall-skinny QRs in one persistent launch; serve: LS serving loop")
     p.add_argument("--kappa", type=float, default=1e2, help="spd: condition number")
     p.add_argument("--count", type=int, default=4096, help="batched: number of matrices")
-    p.add_argument("--rates", type=float, nargs="*", default=None, help="serve: arrival rates (req/s)")
-    p.add_argument("--requests", type=int, default=64, help="serve: requests per rate")
+    p.add_argument("--rates", type=float, nargs="*", default=None,
+                   help="serve: arrival rates as multiples of the measured one-at-a-time rate")
+    p.add_argument("--requests", type=int, default=1000, help="serve: requests per rate")
     p.add_argument("--slots", type=int, default=4, help="serve: server slots")
     p.add_argument("--gemm", type=int, nargs=3, metavar=("M", "N", "K"), default=None,
                    help="time only the tensor-core GEMM R12 = Q1^T A2 of this shape (TN, FP16) — the "
@@ -135,6 +139,29 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+# ----------------------------------------------------------- FP64 metrics
+def qr_errors_fp64(A, Q, R, block=2048):
+    """||A - QR||_F / ||A||_F and ||I - Q^T Q||_F with FP64 products on the GPU, in column blocks
+    (R upper triangular: block J of A - QR needs Q[:, :J_end]; Q^T Q symmetric: blocks on and above
+    the diagonal, off-diagonal ones counted twice)."""
+    import torch
+    m, n = Q.shape
+    Qd = Q.double()
+    num = torch.zeros((), dtype=torch.float64, device=Q.device)
+    den = torch.zeros((), dtype=torch.float64, device=Q.device)
+    orth = torch.zeros((), dtype=torch.float64, device=Q.device)
+    for j0 in range(0, n, block):
+        j1 = min(n, j0 + block)
+        Ab = A[:, j0:j1].double()
+        res = Ab - Qd[:, :j1] @ torch.triu(R[:j1, j0:j1].double(), diagonal=-j0)
+        num += (res * res).sum()
+        den += (Ab * Ab).sum()
+        G = Qd[:, j0:j1].t() @ Qd[:, j0:]
+        G[:, : j1 - j0] -= torch.eye(j1 - j0, dtype=torch.float64, device=Q.device)
+        orth += (G[:, : j1 - j0] ** 2).sum() + 2.0 * (G[:, j1 - j0:] ** 2).sum()
+    return float(torch.sqrt(num / den)), float(torch.sqrt(orth))
+
+
 # ------------------------------------------------------------ CPU baselines
 def cpu_oracle_rate(m, n, seed, prec="fp16"):
     """Times the oracle restatement of later_rgsqrf (numpy, all host threads) on an m x n sample;
@@ -165,10 +192,138 @@ def host_sgeqrf_rate(m, n, seed):
     return qr_flops(m, n) / dt / 1e12, dt
 
 
+def time_reference_gpu(a, A0, ref, steps, warmup, clocks=False):
+    """The reference LATER's rgsqrf on this GPU (oracle/_ref: its kernels compiled from its sources,
+    its host recursion restated call for call with the same cuBLAS calls) on the device matrix A0:
+    device-timed steps, FP64 accuracy of the last one, and the end-to-end time with the matrix copied
+    from pinned host memory and Q, R copied back."""
+    import torch
+    m, n = A0.shape
+    dev = A0.device
+    A = torch.empty(n, m, device=dev).t()
+    R = torch.zeros(n, n, device=dev).t()
+    lw, lh = ref.rgsqrf_bufsize(m, n)
+    work = torch.zeros(max(lw, m // 256 * 32 * 64), device=dev)
+    hwork = torch.zeros(lh, dtype=torch.float16, device=dev)
+    st = torch.cuda.current_stream()
+    for _ in range(warmup):
+        A.copy_(A0)
+        ref.rgsqrf(A, R, work, hwork)
+    torch.cuda.synchronize()
+    evs = []
+    clk = ClockSampler(dev.index or 0) if clocks else None
+    if clk:
+        clk.__enter__()
+    for _ in range(steps):
+        A.copy_(A0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        ref.rgsqrf(A, R, work, hwork)
+        e1.record(st)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    if clk:
+        clk.__exit__()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
+    bwd, orth = qr_errors_fp64(A0, A, torch.triu(R))
+    hA = torch.empty(n, m, pin_memory=True).t()
+    hA.copy_(A0)
+    hQ = torch.empty(n, m, pin_memory=True).t()
+    hR = torch.empty(n, n, pin_memory=True).t()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    k = max(1, min(steps, 3))
+    for _ in range(k):
+        A.copy_(hA, non_blocking=True)
+        ref.rgsqrf(A, R, work, hwork)
+        hQ.copy_(A, non_blocking=True)
+        hR.copy_(R, non_blocking=True)
+    e1.record(st)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / k
+    out = {"ms_per_step": ms, "value": qr_flops(m, n) / ms / 1e9, "unit": "TFLOP/s",
+           "backward_error": bwd, "orthogonality_over_n": orth / n, "e2e_ms": e2e_ms,
+           "e2e": qr_flops(m, n) / e2e_ms / 1e9}
+    if clk:
+        out["clocks"] = clk.summary()
+    return out
+
+
+def time_cusolver_sgeqrf(A0, ref, steps=3):
+    """cusolverDnSgeqrf on the same matrix: the reference QR test's own FP32 GPU comparator
+    (test/test_qr.cu:184-206). Math mode default: FP32 arithmetic, no TF32."""
+    import torch
+    m, n = A0.shape
+    A = torch.empty(n, m, device=A0.device).t()
+    A.copy_(A0)
+    tau = torch.empty(n, device=A0.device)
+    lw = ref.sgeqrf_bufsize(A)
+    work = torch.empty(max(1, lw), device=A0.device)
+    info = torch.zeros(1, dtype=torch.int32, device=A0.device)
+    st = torch.cuda.current_stream()
+    ref.sgeqrf(A, tau, work, info)
+    ts = []
+    for _ in range(steps):
+        A.copy_(A0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        ref.sgeqrf(A, tau, work, info)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    ms = statistics.median(ts)
+    return {"impl": "cusolverDnSgeqrf FP32 (test/test_qr.cu:184-206)", "ms_per_step": ms,
+            "value": qr_flops(m, n) / ms / 1e9, "unit": "TFLOP/s", "info": int(info.item())}
+
+
+def reference_gpu_harness():
+    """The reference LATER on this GPU, or None (not built / no device)."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        from oracle import build_ref
+        if not build_ref.available():
+            build_ref.build()
+        return build_ref.load()
+    except Exception as e:  # noqa: BLE001
+        print(f"reference harness unavailable: {e}", file=sys.stderr)
+        return None
+
+
 def run_reference(a, rank, world):
+    """The reference arm. On a GPU with oracle/_ref built: the reference LATER's own rgsqrf (its
+    kernels and cuBLAS, FP16 tensor-core GEMMs, the only mode it has) on the same 16384^2 matrix,
+    timed like our arm. Otherwise the oracle's port of it on the host cores, on a bounded sample."""
     if rank != 0:
         return
     ncores = os.cpu_count() or 1
+    ref = reference_gpu_harness()
+    if ref is not None:
+        import torch
+        torch.cuda.set_device(0)
+        g = torch.Generator(device="cuda").manual_seed(a.seed)
+        A0 = torch.randn(a.n, a.m, generator=g, device="cuda").t()
+        r = time_reference_gpu(a, A0, ref, a.steps, a.warmup, clocks=True)
+        cfg = workload_config(a)
+        cfg = dict(cfg, workload=f"rgsqrf {a.m}x{a.n} fp32, N(0,1) seed {a.seed}, the reference's FP16 "
+                                 f"tensor-core trailing updates (cuBLAS GemmEx), leaf 128", precision="fp16")
+        sample = ("the reference LATER on this GPU: its mgs_kernel2 / s2h kernels compiled from its sources "
+                  "(oracle/_ref cubins), its host recursion (QR/later_rgsqrf.cu, QR/panel.cu) restated call for "
+                  "call with the same cuBLAS GemmEx / Sgemm / SgemmStridedBatched calls; full matrix")
+        line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "TFLOP/s", "n_gpus": 1,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "fp16", "data": "synthetic", "config": cfg,
+                "accuracy": {"backward_error": r["backward_error"], "orthogonality_over_n": r["orthogonality_over_n"],
+                             "computed": "FP64 on the GPU"},
+                "cpu_baseline": {"value": r["value"], "unit": "TFLOP/s", "cores": ncores, "kind": "reference",
+                                 "device": "GPU", "sample": sample},
+                "e2e": {"value": r["e2e"], "unit": "TFLOP/s", "ms_per_step": r["e2e_ms"],
+                        "h2d_bytes_per_step": a.m * a.n * 4, "d2h_bytes_per_step": a.m * a.n * 4 + a.n * a.n * 4},
+                "clocks": r.get("clocks")}
+        print(json.dumps(line), flush=True)
+        return
     rates = []
     for _ in range(a.warmup):
         cpu_oracle_rate(a.cpu_m, a.cpu_n, a.seed)
@@ -181,7 +336,11 @@ def run_reference(a, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": qr_flops(a.cpu_m, a.cpu_n) / v / 1e9,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp16",
-            "data": "synthetic", "config": workload_config(a),
+            "data": "synthetic",
+            "config": {"workload": f"rgsqrf {a.cpu_m}x{a.cpu_n} fp32 sample, N(0,1) seed {a.seed}, FP16-rounded "
+                                   f"GEMM operands (the reference's arithmetic), leaf 128, on the host cores",
+                       "m": a.cpu_m, "n": a.cpu_n, "precision": "fp16", "leaf": 128,
+                       "sample_of": workload_config(a)["workload"]},
             "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": ncores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -248,13 +407,10 @@ def run_ours(a, rank, world, local_rank):
     ms_step = sum(ms) / len(ms)
     clocks = clk.summary()
 
-    # ---- accuracy of the last step (FP32 on the GPU, TF32 off, like the reference's checker)
-    torch.backends.cuda.matmul.allow_tf32 = False
-    Rt = torch.triu(R)
-    res = (A0 - A @ Rt).norm() / A0.norm()
-    eye = torch.eye(n, device=dev)
-    orth = (eye - A.t() @ A).norm()
-    bwd, orth = float(res), float(orth)
+    # ---- accuracy of the last step, in FP64 on the GPU (outside the timed region)
+    t_acc = time.perf_counter()
+    bwd, orth = qr_errors_fp64(A0, A, R)
+    t_acc = time.perf_counter() - t_acc
 
     # ---- the same matrix in a second precision (the reference's FP16 by default)
     alt = None
@@ -280,11 +436,27 @@ def run_ours(a, rank, world, local_rank):
             e1.record(st)
             torch.cuda.synchronize()
             ms_alt.append(e0.elapsed_time(e1))
-        bwd_alt = float((A0 - A @ torch.triu(R)).norm() / A0.norm())
-        orth_alt = float((eye - A.t() @ A).norm())
+        bwd_alt, orth_alt = qr_errors_fp64(A0, A, R)
         ma = sum(ms_alt) / len(ms_alt)
         alt = {a.alt_precision: {"value": flops / ma / 1e9, "unit": "TFLOP/s", "ms_per_step": ma,
                                  "steps": a.steps, "backward_error": bwd_alt, "orthogonality_over_n": orth_alt / n}}
+
+    # ---- the reference LATER and cuSOLVER's Sgeqrf on the same matrix and GPU, in this process
+    same_gpu = None
+    if not a.no_ref:
+        ref = reference_gpu_harness()
+        if ref is not None:
+            try:
+                rr = time_reference_gpu(a, A0, ref, a.steps, 2)
+                rr["impl"] = ("reference LATER rgsqrf: its kernels (compiled from its sources) + its host recursion "
+                              "restated with the same cuBLAS calls, FP16 GemmEx")
+                same_gpu = {"reference_rgsqrf": rr, "cusolver_sgeqrf": time_cusolver_sgeqrf(A0, ref)}
+                same_gpu["speedup_vs_reference"] = rr["ms_per_step"] / ms_step
+                same_gpu["e2e_speedup_vs_reference"] = None
+            except Exception as e:  # noqa: BLE001
+                same_gpu = {"error": str(e)}
+        else:
+            same_gpu = {"unavailable": "oracle/_ref not built"}
 
     # ---- per-class trace of one extra step (roofline of the dominant kernel)
     A.copy_(A0)
@@ -295,7 +467,8 @@ def run_ours(a, rank, world, local_rank):
     # ---- end to end through the public API: pinned host A in, Q and R out
     e2e = None
     if a.e2e_steps > 0:
-        hA = A0.cpu().pin_memory()
+        hA = torch.empty(n, m, pin_memory=True).t()  # column-major like A: one contiguous copy each way
+        hA.copy_(A0)
         hQ = torch.empty(n, m, pin_memory=True).t()
         hR = torch.empty(n, n, pin_memory=True).t()
         torch.cuda.synchronize()
@@ -312,6 +485,9 @@ def run_ours(a, rank, world, local_rank):
         e2e_ms = e0.elapsed_time(e1) / a.e2e_steps
         e2e = {"value": flops / e2e_ms / 1e9, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
                "h2d_bytes_per_step": m * n * 4, "d2h_bytes_per_step": m * n * 4 + n * n * 4}
+
+    if same_gpu and e2e and "reference_rgsqrf" in same_gpu:
+        same_gpu["e2e_speedup_vs_reference"] = same_gpu["reference_rgsqrf"]["e2e_ms"] / e2e["ms_per_step"]
 
     # ---- aggregate over ranks (max time)
     rate = flops / ms_step / 1e9
@@ -383,13 +559,36 @@ def run_ours(a, rank, world, local_rank):
             "vs_baseline": None, "dtype": a.precision, "data": "synthetic",
             "config": workload_config(a),
             "accuracy": {"backward_error": bwd, "orthogonality_fro": orth, "orthogonality_over_n": orth / n,
-                         "computed": "FP32 on GPU, TF32 off (as test/test_qr.cu:216-268)"},
+                         "computed": "FP64 on the GPU (the quantities of test/test_qr.cu:216-268 without the "
+                                     "FP32 checker's own rounding)", "seconds": t_acc},
             "executed_tflops": 2.0 * m * n * n / ms_step / 1e9, "alt_precision": alt,
-            "roofline": roof, "roofline_gemm": roof_gemm, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "roofline": roof, "roofline_gemm": roof_gemm, "cpu_baseline": cpu, "e2e": e2e,
+            "same_gpu_comparators": same_gpu, "gpu_launches": launches,
             "launches_per_step": launches / max(1, a.steps), "clocks": clocks,
             "wall_s_timed_region": t_wall,
             "trace_ms": {"gemm": tr["gemm_ms"], "panel": tr["panel_ms"], "leaf_gemm": tr["leaf_gemm_ms"],
                          "other": tr["other_ms"]}}
+    if world == 1 and not a.no_extras:
+        # The other configurations of the reference's workload, measured in the same run (each with its
+        # own roofline): C3 Cholesky + refined SPD solve, C4 batched uneven QR, C5 least-squares serving.
+        del A, A0, R, work, hwork
+        torch.cuda.empty_cache()
+        ref = None if a.no_ref else reference_gpu_harness()
+        extras = {}
+        t_x = time.perf_counter()
+        for name, fn in (("C3_spd_kappa1e2", lambda: spd_result(a, 16384, 1e2, "fp16", 3, 1, cpu=not a.no_cpu, ref=ref)),
+                         ("C3_spd_kappa1e6", lambda: spd_result(a, 16384, 1e6, "fp16", 3, 1, cpu=False, ref=None)),
+                         ("C4_batched", lambda: batched_result(a, 4096, 3, 2)),
+                         ("C5_serve", lambda: serve_result(a, 1000, [0.5, 2.0, 8.0], 4, 200))):
+            t1 = time.perf_counter()
+            try:
+                extras[name] = fn()
+            except Exception as e:  # noqa: BLE001
+                extras[name] = {"error": f"{type(e).__name__}: {e}"}
+            extras[name]["wall_s"] = time.perf_counter() - t1
+            torch.cuda.empty_cache()
+        line["configs"] = extras
+        line["configs_wall_s"] = time.perf_counter() - t_x
     print(json.dumps(line), flush=True)
 
 
@@ -425,88 +624,159 @@ def _haar_gpu(n, k, g):
     return q * torch.sign(torch.diagonal(r))[None, :]
 
 
-def run_spd(a):
+def _peaks():
+    pk = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(pk.read_text()) if pk.exists() else {}
+
+
+def spd_result(a, n, kappa, precision, steps, warmup, cpu=True, ref=None):
     """Config 3: n x n SPD A = Q diag(lambda) Q^T (Q Haar, lambda log-uniform in [1/kappa, 1]),
     rpotrf + FP64 iterative refinement on 16 FP32 right-hand sides to backward error 1e-12."""
     import numpy as np
     import torch
     import later_gb300 as lg
-    n, k = a.n, 16
+    k = 16
     g = torch.Generator(device="cuda").manual_seed(a.seed)
     # Q from an FP32 QR (an FP64 QR of n=16384 is slow on GB300's FP64 units); A = Q diag(lam) Q^T is formed
     # in FP64, so A is a congruence of diag(lam) by a near-orthogonal Q (spectrum within ~1e-5 relative) and
     # only its final rounding to FP32 perturbs it. An FP32 product would add accumulation error far above
     # lam_min = 1/kappa at kappa = 1e6.
+    t_gen = time.perf_counter()
     q, r = torch.linalg.qr(torch.randn(n, n, generator=g, device="cuda"))
     q *= torch.sign(torch.diagonal(r))[None, :]
     del r
     q = q.double()
-    lam = torch.exp(torch.empty(n, device="cuda", dtype=torch.float64).uniform_(-float(np.log(a.kappa)), 0.0,
+    lam = torch.exp(torch.empty(n, device="cuda", dtype=torch.float64).uniform_(-float(np.log(kappa)), 0.0,
                                                                                  generator=g))
     A = (q * lam[None, :]) @ q.t()
     del q
     A = lg.colmajor(((A + A.t()) / 2).float())
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t_gen
     B = lg.colmajor(torch.randn(n, k, generator=g, device="cuda"))
     F = lg.empty_colmajor(n, n)
-    lw, lh = lg.blas3_bufsize("p", n, n, precision=a.precision)
+    lw, lh = lg.blas3_bufsize("p", n, n, precision=precision)
     work = torch.empty(lw, dtype=torch.float32, device="cuda")
     hwork = torch.empty(lh, dtype=torch.float16, device="cuda")
-    ts, infos = [], []
-    for it in range(a.warmup + a.steps):
+    ts = []
+    st = 0
+    for it in range(warmup + steps):
         F.copy_(A)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        lg.later_rpotrf("l", n, F, precision=a.precision, work=work, hwork=hwork)
+        lg.later_rpotrf("l", n, F, precision=precision, work=work, hwork=hwork)
         e1.record()
         torch.cuda.synchronize()
         st = lg.device_status()
-        if it >= a.warmup:
+        if it >= warmup:
             ts.append(e0.elapsed_time(e1))
     fact_ms = statistics.median(ts)
+    del work, hwork
     t0 = time.perf_counter()
-    X, info = lg.spd_solve(A, B, precision=a.precision, max_iter=50, tol=1e-12)
+    X, info = lg.spd_solve(A, B, precision=precision, max_iter=60, tol=1e-12)
+    torch.cuda.synchronize()
     solve_s = time.perf_counter() - t0
     flops = n ** 3 / 3.0
-    cpu = None
-    if not a.no_cpu:
+    peak = _peaks().get("bf16_tflops") or 1900.0
+    ach = flops / fact_ms / 1e9
+    out = {"workload": f"rpotrf n={n} SPD kappa={kappa:g} ({precision} tensor-core updates) + FP64 refinement, "
+                       f"{k} RHS to backward error 1e-12",
+           "value": ach, "unit": "TFLOP/s (n^3/3)", "ms_per_step": fact_ms, "steps": steps,
+           "factor_status": st, "solve": {"seconds_incl_factor": solve_s, **info},
+           "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                        "peak_source": "measured bf16 burst (MEASURED_PEAKS.json)"},
+           "input_build_s": t_gen}
+    if ref is not None:  # the reference's l_potrf (cuSOLVER Spotrf leaves + its rtrsm / rsyrk) and cuSOLVER
+        try:
+            Fr = lg.empty_colmajor(n, n)
+            hw = torch.zeros(n // 2 * n, dtype=torch.float16, device="cuda")
+            rts = []
+            for it in range(3):
+                Fr.copy_(A)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                infor = ref.rpotrf(Fr, hw)
+                e1.record()
+                torch.cuda.synchronize()
+                if it:
+                    rts.append(e0.elapsed_time(e1))
+            rms = statistics.median(rts)
+            lwc = ref.spotrf_bufsize(Fr)
+            wc = torch.empty(max(1, lwc), device="cuda")
+            dinfo = torch.zeros(1, dtype=torch.int32, device="cuda")
+            cts = []
+            for it in range(3):
+                Fr.copy_(A)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                ref.spotrf(Fr, wc, dinfo)
+                e1.record()
+                torch.cuda.synchronize()
+                if it:
+                    cts.append(e0.elapsed_time(e1))
+            cms = statistics.median(cts)
+            out["same_gpu_comparators"] = {
+                "reference_rpotrf": {"ms_per_step": rms, "value": flops / rms / 1e9, "info": infor,
+                                     "impl": "reference l_potrf: cusolverDnSpotrf leaves of 2048 (LWORK 65536), "
+                                             "its recursive trsm / syrk with FP16 GemmEx"},
+                "cusolver_spotrf": {"ms_per_step": cms, "value": flops / cms / 1e9, "info": int(dinfo.item()),
+                                    "impl": "cusolverDnSpotrf FP32"}}
+            del Fr, hw, wc
+        except Exception as e:  # noqa: BLE001
+            out["same_gpu_comparators"] = {"error": str(e)}
+    if cpu:
         import scipy.linalg.lapack as la
-        ns = n
         As = np.asfortranarray(A.cpu().numpy())
         la.spotrf(As[:512, :512].copy(order="F"))
         t = time.perf_counter()
         la.spotrf(As, lower=1, overwrite_a=1)
         dt = time.perf_counter() - t
-        cpu = {"value": ns ** 3 / 3.0 / dt / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"host LAPACK spotrf (scipy's OpenBLAS, all host cores) on the same {ns}x{ns} matrix, {dt:.2f} s"}
-    print(json.dumps({"metric": "Cholesky TFLOP/s (n^3/3) + refined SPD solve", "value": flops / fact_ms / 1e9,
+        out["cpu_baseline"] = {"value": flops / dt / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": f"host LAPACK spotrf (scipy's OpenBLAS, all host cores) on "
+                                                         f"the same {n}x{n} matrix, {dt:.2f} s"}
+    return out
+
+
+def run_spd(a):
+    r = spd_result(a, a.n, a.kappa, a.precision, a.steps, a.warmup, cpu=not a.no_cpu,
+                   ref=None if a.no_ref else reference_gpu_harness())
+    print(json.dumps({"metric": "Cholesky TFLOP/s (n^3/3) + refined SPD solve", "value": r["value"],
                       "unit": "TFLOP/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
-                      "ms_per_step": fact_ms, "higher_is_better": True, "dtype": a.precision, "data": "synthetic",
-                      "config": {"workload": f"rpotrf n={n} SPD kappa={a.kappa:g} + FP64 refinement, 16 RHS",
-                                 "n": n, "kappa": a.kappa, "precision": a.precision},
-                      "factor_status": st, "solve": {"seconds_incl_factor": solve_s, **info},
-                      "cpu_baseline": cpu}), flush=True)
+                      "ms_per_step": r["ms_per_step"], "higher_is_better": True, "dtype": a.precision,
+                      "data": "synthetic", "config": {"workload": r["workload"], "n": a.n, "kappa": a.kappa,
+                                                      "precision": a.precision}, **{k: v for k, v in r.items()
+                                                      if k not in ("value", "ms_per_step", "workload")}}),
+          flush=True)
 
 
-def run_batched(a):
-    """Config 4: `count` N(0,1) matrices, m log-uniform [256, 8192], n log-uniform [16, 256], m >= 4n;
-    one persistent launch under a captured CUDA graph, tile variant from the autotuner; compared with
-    looping plain rgsqrf per matrix (timed on a sample of the same distribution)."""
+def batched_shapes(count, seed):
     import numpy as np
-    import torch
-    import later_gb300 as lg
-    from later_gb300 import autotune
-    rng = np.random.default_rng(a.seed)
+    rng = np.random.default_rng(seed)
     shapes = []
-    while len(shapes) < a.count:
+    while len(shapes) < count:
         m = int(np.exp(rng.uniform(np.log(256), np.log(8192))))
         n = int(np.exp(rng.uniform(np.log(16), np.log(256))))
         if m >= 4 * n:
             shapes.append((m, n))
+    return shapes
+
+
+def batched_result(a, count, steps, warmup):
+    """Config 4: `count` N(0,1) matrices, m log-uniform [256, 8192], n log-uniform [16, 256], m >= 4n;
+    one persistent launch under a captured CUDA graph, tile variant from the autotuner; compared with
+    looping plain rgsqrf per matrix (timed on a sample of the same distribution)."""
+    import torch
+    import later_gb300 as lg
+    from later_gb300 import autotune
+    shapes = batched_shapes(count, a.seed)
     g = torch.Generator(device="cuda").manual_seed(a.seed)
     orig = [torch.randn(n, m, generator=g, device="cuda").t() for m, n in shapes]
     mats = [o.clone() for o in orig]
     flops = sum(2.0 * n * n * (m - n / 3.0) for m, n in shapes)
+    nbytes = sum(4.0 * (2 * m * n + n * n) for m, n in shapes)  # read A, write Q, write R
     best, tune_ms = autotune.tune(shapes, use_cache=True)
     b = lg.BatchedQR(mats)
     s = torch.cuda.Stream()
@@ -518,7 +788,7 @@ def run_batched(a):
         with torch.cuda.graph(graph, stream=s):
             b.run(best, stream=s)
     ts = []
-    for it in range(a.warmup + a.steps):
+    for it in range(warmup + steps):
         for x, o in zip(mats, orig):
             x.copy_(o)
         torch.cuda.synchronize()
@@ -527,12 +797,12 @@ def run_batched(a):
         graph.replay()
         e1.record()
         torch.cuda.synchronize()
-        if it >= a.warmup:
+        if it >= warmup:
             ts.append(e0.elapsed_time(e1))
     ms = statistics.median(ts)
     bad = int((b.status != 0).sum())
     # comparator: plain rgsqrf per matrix on a sample of 256, scaled by flops
-    idx = list(range(0, a.count, max(1, a.count // 256)))
+    idx = list(range(0, count, max(1, count // 256)))
     sub = [orig[i].clone() for i in idx]
     for x in sub[:4]:
         lg.later_rgsqrf(x.clone())
@@ -543,19 +813,27 @@ def run_batched(a):
     torch.cuda.synchronize()
     loop_s = time.perf_counter() - t0
     sub_flops = sum(2.0 * shapes[i][1] ** 2 * (shapes[i][0] - shapes[i][1] / 3.0) for i in idx)
-    print(json.dumps({"metric": "batched QR TFLOP/s (sum 2n^2(m-n/3)) and matrices/s", "value": flops / ms / 1e9,
-                      "unit": "TFLOP/s", "matrices_per_s": a.count / ms * 1e3, "ms_per_step": ms,
-                      "n_gpus": 1, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True,
-                      "dtype": "fp32", "data": "synthetic", "graph": True, "variant": best, "autotune_ms": tune_ms,
-                      "matrices_failed": bad,
-                      "config": {"workload": f"{a.count} N(0,1) matrices, m in [256,8192], n in [16,256], m>=4n"},
-                      "comparator_rgsqrf_loop": {"value": sub_flops / loop_s / 1e12, "unit": "TFLOP/s",
-                                                 "matrices_per_s": len(sub) / loop_s,
-                                                 "sample": f"{len(sub)} matrices of the same distribution"}}),
-          flush=True)
+    hbm = _peaks().get("hbm_gbs") or 6800.0
+    gbs = nbytes / ms / 1e6
+    return {"workload": f"{count} N(0,1) matrices, m in [256,8192], n in [16,256], m>=4n; one persistent launch "
+                        f"in a captured CUDA graph", "value": flops / ms / 1e9, "unit": "TFLOP/s (sum 2n^2(m-n/3))",
+            "matrices_per_s": count / ms * 1e3, "ms_per_step": ms, "steps": steps, "graph": True, "variant": best,
+            "autotune_ms": tune_ms, "matrices_failed": bad,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                         "algorithmic_bytes": nbytes, "note": "read A, write Q and R once; FP32 SIMT arithmetic"},
+            "comparator_rgsqrf_loop": {"value": sub_flops / loop_s / 1e12, "unit": "TFLOP/s",
+                                       "matrices_per_s": len(sub) / loop_s,
+                                       "sample": f"{len(sub)} matrices of the same distribution"}}
 
 
-def run_serve(a):
+def run_batched(a):
+    r = batched_result(a, a.count, a.steps, a.warmup)
+    print(json.dumps({"metric": "batched QR TFLOP/s (sum 2n^2(m-n/3)) and matrices/s", "n_gpus": 1,
+                      "warmup": a.warmup, "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
+                      "config": {"workload": r["workload"]}, **r}), flush=True)
+
+
+def serve_result(a, requests, rates_factors, slots, base_requests):
     """Config 5: Poisson arrivals of LS requests, m log-uniform [512, 32768], n log-uniform [32, 2048],
     m >= 2n, kappa log-uniform [1e1, 1e4] (SVD construction), b = A x* + 1e-3 noise; refinement to
     backward error 1e-6; solves/s and p50/p99 latency at each swept rate, against an FP32 QR least-squares
@@ -567,7 +845,7 @@ def run_serve(a):
     rng = np.random.default_rng(a.seed)
     g = torch.Generator(device="cuda").manual_seed(a.seed)
     pool = []
-    npool = min(a.requests, 32)
+    npool = min(requests, 32)
     while len(pool) < npool:
         m = int(np.exp(rng.uniform(np.log(512), np.log(32768))))
         n = int(np.exp(rng.uniform(np.log(32), np.log(2048))))
@@ -581,19 +859,18 @@ def run_serve(a):
         xs = torch.randn(n, 1, generator=g, device="cuda", dtype=torch.float64)
         B = (A.double() @ xs + 1e-3 * torch.randn(m, 1, generator=g, device="cuda", dtype=torch.float64)).float()
         pool.append((np.asfortranarray(A.cpu().numpy()), np.asfortranarray(B.cpu().numpy())))
-    # capacity estimate: one request at a time
-    srv = lg.LsServer(slots=a.slots, hbm_budget_gb=64, precision="split3", tol=1e-6)
+    req_flops = [2.0 * A.shape[1] ** 2 * (A.shape[0] - A.shape[1] / 3.0) for A, _ in pool]
+    srv = lg.LsServer(slots=slots, hbm_budget_gb=64, precision="split3", tol=1e-6)
     for A, B in pool[:2]:
         srv.wait(srv.submit(A, B))
     t0 = time.perf_counter()
     for A, B in pool[:8]:
         srv.wait(srv.submit(A, B))
     serial = (time.perf_counter() - t0) / 8
-    # from half the serial rate up to well past saturation (the top rates measure capacity)
-    rates = a.rates or [f / serial for f in (0.5, 1.0, 2.0, 4.0, 8.0, 16.0)]
+    rates = [f / serial for f in rates_factors]
     results = []
     for lam in rates:
-        arr = np.cumsum(rng.exponential(1.0 / lam, a.requests))
+        arr = np.cumsum(rng.exponential(1.0 / lam, requests))
         t_start = time.perf_counter()
         tickets = []
         for i, t_arr in enumerate(arr):
@@ -606,34 +883,47 @@ def run_serve(a):
         wall = time.perf_counter() - t_start
         lat = np.array([r["latency_ms"] for _, r in outs])
         bwd = max(r["backward_error"] for _, r in outs)
-        results.append({"rate": lam, "solves_per_s": len(outs) / wall, "p50_ms": float(np.percentile(lat, 50)),
-                        "p99_ms": float(np.percentile(lat, 99)), "max_backward_error": bwd,
-                        "failed": sum(1 for _, r in outs if r["status"] != 0)})
+        results.append({"rate": lam, "requests": requests, "solves_per_s": len(outs) / wall,
+                        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                        "max_backward_error": bwd, "failed": sum(1 for _, r in outs if r["status"] != 0),
+                        "qr_tflops": sum(req_flops[i % len(pool)] for i in range(requests)) / wall / 1e12})
+    peak_hbm = srv.hbm_peak()
     srv.close()
-    # FP32 QR baseline on the same GPU, same stream at the highest rate, one request at a time
-    base = []
+    # FP32 QR baseline on the same GPU, same request pool, one request at a time
     for A, B in pool[:2]:
         torch.linalg.lstsq(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda())
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     lat = []
-    for i in range(a.requests):
+    for i in range(base_requests):
         A, B = pool[i % len(pool)]
         t1 = time.perf_counter()
         x = torch.linalg.lstsq(torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()).solution
         x.cpu()
         lat.append((time.perf_counter() - t1) * 1e3)
     wall = time.perf_counter() - t0
-    base = {"solves_per_s": a.requests / wall, "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)),
+    base = {"solves_per_s": base_requests / wall, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "requests": base_requests,
             "impl": "torch.linalg.lstsq FP32 on the GPU (cuSOLVER QR), serial"}
     best = max(results, key=lambda r: r["solves_per_s"])
-    print(json.dumps({"metric": "LS solves/s at backward error <= 1e-6, p50/p99 latency", "value": best["solves_per_s"],
-                      "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "split3",
-                      "data": "synthetic", "slots": a.slots, "sweep": results, "fp32_qr_baseline": base,
-                      "config": {"workload": f"{a.requests} LS requests per rate from a pool of {len(pool)}, "
-                                             "m in [512,32768], n in [32,2048], m>=2n, kappa in [1e1,1e4]"}}),
-          flush=True)
+    peak = _peaks().get("bf16_tflops") or 1900.0
+    return {"workload": f"{requests} LS requests per rate from a pool of {len(pool)}, m in [512,32768], "
+                        f"n in [32,2048], m>=2n, kappa in [1e1,1e4], {slots} slots",
+            "value": best["solves_per_s"], "unit": "solves/s", "slots": slots, "sweep": results,
+            "fp32_qr_baseline": base, "speedup_vs_fp32_qr": best["solves_per_s"] / base["solves_per_s"],
+            "hbm_peak_bytes": peak_hbm,
+            "roofline": {"bound": "tensor", "achieved": best["qr_tflops"], "peak": peak, "unit": "TFLOP/s",
+                         "frac": best["qr_tflops"] / peak,
+                         "note": "QR flops 2n^2(m-n/3) of the solved requests per second at the best rate; "
+                                 "small requests are launch- and latency-bound"}}
+
+
+def run_serve(a):
+    factors = [r for r in a.rates] if a.rates else [0.5, 1.0, 2.0, 4.0, 8.0, 16.0]
+    r = serve_result(a, a.requests, factors, a.slots, min(a.requests, 200))
+    print(json.dumps({"metric": "LS solves/s at backward error <= 1e-6, p50/p99 latency", "n_gpus": 1,
+                      "higher_is_better": True, "dtype": "split3", "data": "synthetic",
+                      "config": {"workload": r["workload"]}, **r}), flush=True)
 
 
 def main():

@@ -19,9 +19,13 @@
  *     does not link cuBLAS), else on the default stream;
  *   - any lda >= m is honoured; R is written in full, zeros below the diagonal;
  *   - rtrsm / rsyrk / rtrmm / rpotrf, whose reference signatures carry no
- *     workspace sizes, use a library-owned per-device workspace (grown when a
- *     larger problem arrives) instead of the caller's `work` / `hwork`; the C
- *     ABI (later_c.h) takes explicit workspaces and never allocates.
+ *     workspace sizes, use a library-owned workspace per (device, stream)
+ *     instead of the caller's `work` / `hwork`. It grows when a larger
+ *     problem arrives on that stream (cudaMallocAsync / cudaFreeAsync on the
+ *     same stream, so no device-wide synchronisation) and is kept until exit.
+ *     Calls from several host threads are safe: each stream has its own
+ *     buffers, and calls on one stream use them in stream order. The C ABI
+ *     (later_c.h) takes explicit workspaces and never allocates.
  * The helper functions of the reference header (timers, generators, s2h and
  * friends, the out-of-core / EVD / blocked routines) are outside this
  * library's scope and are not declared here.

@@ -65,6 +65,17 @@ const char* later_c_status_string(later_status_t s);
 /* Synchronises `stream`, then returns and clears the device status word. */
 later_status_t later_c_device_status(later_stream_t stream);
 
+/*
+ * Failure-detection self-check (no counterpart in the reference, which has no
+ * bounded waits): enqueues one small kernel whose two device waits, on an
+ * mbarrier phase and on a global flag that nothing ever completes, give up
+ * after `timeout_cycles` SM cycles (0 = the default of about one second). The
+ * next later_c_device_status on the stream then returns LATER_ERR_TIMEOUT, and
+ * the context stays usable: the same path every kernel of the library takes
+ * when one of its waits runs out.
+ */
+later_status_t later_c_wait_selftest(later_stream_t stream, long long timeout_cycles);
+
 /* ------------------------------------------------------------------ QR */
 
 /* Minimum `work` (floats) and `hwork` (16-bit elements) for later_c_rgsqrf. */

@@ -21,7 +21,7 @@ __all__ = [
     "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
     "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "later_rsyrk", "later_rtrsm",
     "later_rtrmm", "later_rpotrf", "blas3_bufsize",
-    "spd_solve", "ls_solve", "BatchedQR", "LsServer", "gemm16", "convert16", "device_status", "launch_count", "trace_begin",
+    "spd_solve", "ls_solve", "BatchedQR", "LsServer", "gemm16", "convert16", "device_status", "wait_selftest", "launch_count", "trace_begin",
     "trace_end",
 ]
 
@@ -90,6 +90,7 @@ _SIGS = {
     "later_c_default_options": (None, [ctypes.POINTER(Options)]),
     "later_c_status_string": (ctypes.c_char_p, [_i]),
     "later_c_device_status": (_i, [_vp]),
+    "later_c_wait_selftest": (_i, [_vp, ctypes.c_longlong]),
     "later_c_rgsqrf_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "later_c_rgsqrf": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_gemm16": (_i, [_vp, ctypes.c_char, ctypes.c_char, _i, _i, _i, _f, _vp, _i, _vp, _i, _f, _vp, _i,
@@ -178,6 +179,12 @@ def _check(status: int, where: str):
 def device_status(stream=None) -> int:
     """Synchronises the stream and returns (and clears) the device status word."""
     return lib().later_c_device_status(_stream(stream))
+
+
+def wait_selftest(timeout_cycles=0, stream=None):
+    """Enqueues the bounded-wait self-check: its waits run out after timeout_cycles and the next
+    device_status() returns 4 (LATER_ERR_TIMEOUT)."""
+    _check(lib().later_c_wait_selftest(_stream(stream), int(timeout_cycles)), "wait_selftest")
 
 
 def launch_count() -> int:

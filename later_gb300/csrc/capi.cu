@@ -49,6 +49,11 @@ later_status_t later_c_device_status(later_stream_t stream) {
   return LATER_OK;
 }
 
+later_status_t later_c_wait_selftest(later_stream_t stream, long long timeout_cycles) {
+  if (timeout_cycles < 0) return LATER_ERR_INVALID_ARG;
+  return wait_selftest(reinterpret_cast<cudaStream_t>(stream), timeout_cycles);
+}
+
 later_status_t later_c_rgsqrf_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork, int64_t* lhwork) {
   if (m < 1 || n < 1 || m < n) return LATER_ERR_INVALID_ARG;
   const QrNeed q = rgsqrf_need(m, n, options_from(opt));

@@ -4,7 +4,9 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "../../include/LATER.h"
 #include "blas3.cuh"
@@ -32,44 +34,52 @@ cudaStream_t stream_of(cublasHandle_t h) {
 }
 
 // Library-owned workspace for the routines whose reference signatures carry
-// no workspace sizes: one float and one 16-bit buffer per device, grown to the
-// largest request seen, kept until exit.
+// no workspace (rtrsm, rsyrk, rtrmm, rpotrf): one float and one 16-bit buffer
+// per (device, stream), grown to the largest request seen on that stream and
+// kept until exit. A call holds the cache lock from the lookup until its work
+// is enqueued, so each buffer is used in its stream's order only: calls on
+// different streams (or host threads with different cuBLAS-handle streams)
+// get different buffers, and a buffer that grows is released with
+// cudaFreeAsync on its own stream, after the work already queued there.
+struct Entry {
+  float* work = nullptr;
+  size_t lwork = 0;
+  void* hwork = nullptr;
+  size_t lhwork = 0;
+};
 struct Cache {
   std::mutex mu;
-  float* work[64] = {};
-  size_t lwork[64] = {};
-  void* hwork[64] = {};
-  size_t lhwork[64] = {};
+  std::map<std::pair<int, cudaStream_t>, Entry> entries;
 };
 Cache& cache() {
   static Cache c;
   return c;
 }
 
-later_status_t cached(int64_t lw, int64_t lh, float** work, void** hwork) {
+template <class Fn>
+later_status_t with_workspace(cudaStream_t st, int64_t lw, int64_t lh, Fn fn) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev >= 64) return LATER_ERR_CUDA;
+  if (cudaGetDevice(&dev) != cudaSuccess) return LATER_ERR_CUDA;
   Cache& c = cache();
   std::lock_guard<std::mutex> g(c.mu);
-  if (static_cast<size_t>(lw) > c.lwork[dev]) {
-    cudaDeviceSynchronize();
-    if (c.work[dev]) cudaFree(c.work[dev]);
-    c.work[dev] = nullptr;
-    c.lwork[dev] = 0;
-    if (cudaMalloc(&c.work[dev], static_cast<size_t>(lw) * sizeof(float)) != cudaSuccess) return LATER_ERR_CUDA;
-    c.lwork[dev] = static_cast<size_t>(lw);
+  Entry& e = c.entries[{dev, st}];
+  if (static_cast<size_t>(lw) > e.lwork) {
+    if (e.work && cudaFreeAsync(e.work, st) != cudaSuccess) return LATER_ERR_CUDA;
+    e.work = nullptr;
+    e.lwork = 0;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&e.work), static_cast<size_t>(lw) * sizeof(float), st) !=
+        cudaSuccess)
+      return LATER_ERR_CUDA;
+    e.lwork = static_cast<size_t>(lw);
   }
-  if (static_cast<size_t>(lh) > c.lhwork[dev]) {
-    cudaDeviceSynchronize();
-    if (c.hwork[dev]) cudaFree(c.hwork[dev]);
-    c.hwork[dev] = nullptr;
-    c.lhwork[dev] = 0;
-    if (cudaMalloc(&c.hwork[dev], static_cast<size_t>(lh) * 2) != cudaSuccess) return LATER_ERR_CUDA;
-    c.lhwork[dev] = static_cast<size_t>(lh);
+  if (static_cast<size_t>(lh) > e.lhwork) {
+    if (e.hwork && cudaFreeAsync(e.hwork, st) != cudaSuccess) return LATER_ERR_CUDA;
+    e.hwork = nullptr;
+    e.lhwork = 0;
+    if (cudaMallocAsync(&e.hwork, static_cast<size_t>(lh) * 2, st) != cudaSuccess) return LATER_ERR_CUDA;
+    e.lhwork = static_cast<size_t>(lh);
   }
-  *work = c.work[dev];
-  *hwork = c.hwork[dev];
-  return LATER_OK;
+  return fn(e.work, static_cast<int64_t>(e.lwork), e.hwork, static_cast<int64_t>(e.lhwork));
 }
 
 }  // namespace
@@ -100,43 +110,37 @@ void later_ormqr2(int m, int n, float* W, int ldw, float* Y, int ldy, float* wor
 void later_rtrsm(cublasHandle_t handle, char uplo, char leri, char trans, int m, int n, float* A, int lda, float* B,
                  int ldb, __half*) {
   const Options o;
-  float* w = nullptr;
-  void* h = nullptr;
-  const int64_t lh = rtrsm_hwork(m, n, leri, o), lw = splitk_work();
-  later_status_t s = cached(lw, lh, &w, &h);
-  if (s == LATER_OK) s = rtrsm(stream_of(handle), uplo, leri, trans, m, n, A, lda, B, ldb, w, lw, h, lh, o);
-  record("later_rtrsm", s);
+  cudaStream_t st = stream_of(handle);
+  record("later_rtrsm", with_workspace(st, splitk_work(), rtrsm_hwork(m, n, leri, o),
+                                       [&](float* w, int64_t lw, void* h, int64_t lh) {
+                                         return rtrsm(st, uplo, leri, trans, m, n, A, lda, B, ldb, w, lw, h, lh, o);
+                                       }));
 }
 
 void later_rsyrk(cublasHandle_t handle, int n, int k, float alpha, float* A, int lda, float beta, float* C, int ldc,
                  __half*) {
   const Options o;
-  float* w = nullptr;
-  void* h = nullptr;
-  const int64_t lh = rsyrk_hwork(n, k, o), lw = splitk_work();
-  later_status_t s = cached(lw, lh, &w, &h);
-  if (s == LATER_OK) s = rsyrk(stream_of(handle), n, k, alpha, A, lda, beta, C, ldc, w, lw, h, lh, o);
-  record("later_rsyrk", s);
+  cudaStream_t st = stream_of(handle);
+  record("later_rsyrk", with_workspace(st, splitk_work(), rsyrk_hwork(n, k, o),
+                                       [&](float* w, int64_t lw, void* h, int64_t lh) {
+                                         return rsyrk(st, n, k, alpha, A, lda, beta, C, ldc, w, lw, h, lh, o);
+                                       }));
 }
 
 void later_rtrmm(int m, int n, float* A, int lda, float* B, int ldb, float* C, int ldc, float* /*tempC*/, __half*) {
   const Options o;
-  float* w = nullptr;
-  void* h = nullptr;
-  const int64_t lh = rtrmm_hwork(m, n, o), lw = splitk_work();
-  later_status_t s = cached(lw, lh, &w, &h);
-  if (s == LATER_OK) s = rtrmm(nullptr, m, n, A, lda, B, ldb, C, ldc, w, lw, h, lh, o);
-  record("later_rtrmm", s);
+  record("later_rtrmm", with_workspace(nullptr, splitk_work(), rtrmm_hwork(m, n, o),
+                                       [&](float* w, int64_t lw, void* h, int64_t lh) {
+                                         return rtrmm(nullptr, m, n, A, lda, B, ldb, C, ldc, w, lw, h, lh, o);
+                                       }));
 }
 
 void later_rpotrf(char uplo, int n, float* A, int lda, float*, __half*) {
   const Options o;
-  float* w = nullptr;
-  void* h = nullptr;
-  const int64_t lh = rpotrf_hwork(n, o), lw = splitk_work();
-  later_status_t s = cached(lw, lh, &w, &h);
-  if (s == LATER_OK) s = rpotrf(nullptr, uplo, n, A, lda, w, lw, h, lh, o);
-  record("later_rpotrf", s);
+  record("later_rpotrf", with_workspace(nullptr, splitk_work(), rpotrf_hwork(n, o),
+                                        [&](float* w, int64_t lw, void* h, int64_t lh) {
+                                          return rpotrf(nullptr, uplo, n, A, lda, w, lw, h, lh, o);
+                                        }));
 }
 
 later_status_t later_get_last_status() { return g_last; }

@@ -18,6 +18,8 @@
 // race on the array and must be serialised by the caller.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "../../include/later_c.h"
 #include "runtime.cuh"
 
@@ -27,19 +29,21 @@ namespace {
 static __device__ __align__(256) float g_noalloc_scratch[LATER_NOALLOC_SCRATCH_FLOATS];
 
 constexpr int kMaxDevices = 64;
-float* g_scratch_ptr[kMaxDevices] = {};
+std::atomic<float*> g_scratch_ptr[kMaxDevices] = {};  // filled on first use per device
 
 // Device address of this device's scratch array (set-up on first use).
 later_status_t scratch_for_current_device(float** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return LATER_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return LATER_ERR_NOT_SUPPORTED;
-  if (!g_scratch_ptr[dev]) {
+  float* ptr = g_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (!ptr) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return LATER_ERR_CUDA;
-    g_scratch_ptr[dev] = static_cast<float*>(p);
+    ptr = static_cast<float*>(p);
+    g_scratch_ptr[dev].store(ptr, std::memory_order_release);
   }
-  *out = g_scratch_ptr[dev];
+  *out = ptr;
   return LATER_OK;
 }
 

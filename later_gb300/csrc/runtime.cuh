@@ -108,6 +108,11 @@ later_status_t copy2d(cudaStream_t st, int m, int n, const float* X, int64_t ldx
 // ------------------------------------------------------------- tracing
 enum TraceKind { TRACE_GEMM = 0, TRACE_PANEL = 1, TRACE_LEAF_GEMM = 2, TRACE_OTHER = 3 };
 void note_launch(int n = 1);
+
+// Launches one kernel whose two bounded waits (an mbarrier phase and a global
+// flag, neither of which ever completes) run out after `budget` cycles and
+// set DEV_TIMEOUT in the device status word.
+later_status_t wait_selftest(cudaStream_t st, long long budget);
 // Brackets the launches issued during its lifetime with CUDA events on `st`
 // while tracing is on (later_c_trace_begin); otherwise does nothing.
 class TraceScope {

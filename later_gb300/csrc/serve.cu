@@ -12,10 +12,11 @@
 // refinement to the requested backward error. Latency is measured per request
 // from submit to completion on the host's steady clock.
 //
-// Concurrency notes: the per-device status word read by the solver is shared,
-// so with several slots an error flag raised by one request can be observed
-// (and cleared) by another request's status check; results are otherwise
-// independent and each request's arithmetic does not depend on the others.
+// Each request has its own device status word (carved with its buffers): the
+// worker thread directs the status reports of the kernels it launches for the
+// request to that word, so a timeout, range or pivot flag raised by one
+// request is seen by that request alone. Each request's arithmetic does not
+// depend on the others.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -94,7 +95,7 @@ struct Job {
 };
 
 struct Layout {
-  size_t a, b, x, work, hwork, total;
+  size_t status, a, b, x, work, hwork, total;
   int64_t lwork, lhwork;
 };
 
@@ -103,6 +104,8 @@ Layout layout_for(const later_ls_request_t& r, const Options& o) {
   const SolveNeed need = ls_solve_need(r.m, r.n, r.nrhs, o);
   auto up = [](size_t v) { return (v + 255) / 256 * 256; };
   size_t off = 0;
+  L.status = off;
+  off += 256;
   L.a = off;
   off += up(sizeof(float) * r.m * static_cast<size_t>(r.n));
   L.b = off;
@@ -155,10 +158,13 @@ void run_job(later_server* s, Job& j, size_t off, const Layout& L, cudaStream_t 
   double* dX = reinterpret_cast<double*>(base + L.x);
   float* dW = reinterpret_cast<float*>(base + L.work);
   void* dH = base + L.hwork;
+  int* status = reinterpret_cast<int*>(base + L.status);
+  ThreadStatusWord own_status(status);  // this request's kernels report here
   later_status_t st_ = LATER_OK;
   auto ck = [&](cudaError_t e) {
     if (e != cudaSuccess && st_ == LATER_OK) st_ = LATER_ERR_CUDA;
   };
+  ck(cudaMemsetAsync(status, 0, sizeof(int), st));
   ck(cudaMemcpy2DAsync(dA, sizeof(float) * r.m, r.A, sizeof(float) * r.lda, sizeof(float) * r.m, r.n,
                        cudaMemcpyHostToDevice, st));
   ck(cudaMemcpy2DAsync(dB, sizeof(float) * r.m, r.B, sizeof(float) * r.ldb, sizeof(float) * r.m, r.nrhs,

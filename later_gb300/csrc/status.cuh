@@ -26,8 +26,24 @@ constexpr long long kDefaultBudgetCycles = 2000000000LL;
 // Bound used while draining operations that are already in flight.
 constexpr long long kDrainBudgetCycles = 4000000000LL;
 
-// Address of this device's status word (set up once per device).
+// Address of the status word the calling host thread's kernels report to: the
+// thread's own word when one is set (set_thread_status_word), else this
+// device's shared word (set up once per device).
 int* device_status_ptr();
+
+// Directs the status reports of the kernels this host thread launches to `p`
+// (nullptr: back to the device's shared word); returns the previous setting.
+int* set_thread_status_word(int* p);
+
+struct ThreadStatusWord {
+  explicit ThreadStatusWord(int* p) : old_(set_thread_status_word(p)) {}
+  ~ThreadStatusWord() { set_thread_status_word(old_); }
+  ThreadStatusWord(const ThreadStatusWord&) = delete;
+  ThreadStatusWord& operator=(const ThreadStatusWord&) = delete;
+
+ private:
+  int* old_;
+};
 int num_sms();
 
 inline later_status_t cuda_status(cudaError_t e) { return e == cudaSuccess ? LATER_OK : LATER_ERR_CUDA; }

@@ -6,39 +6,60 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
+#include "ptx.cuh"
 #include "runtime.cuh"
 
 namespace later {
 
 __device__ int g_device_status;
+// A flag that no code writes: the target of the bounded-wait self-test.
+__device__ int g_never_set;
 
 namespace {
 constexpr int kMaxDev = 64;
-int* g_status_ptr[kMaxDev] = {};
-int g_nsm[kMaxDev] = {};
+// Per-device caches, filled on first use; two threads filling one at the same
+// time store the same value.
+std::atomic<int*> g_status_ptr[kMaxDev] = {};
+std::atomic<int> g_nsm[kMaxDev] = {};
+// A host thread may direct the status reports of the kernels it launches to a
+// word of its own (the serving loop gives each request one).
+thread_local int* t_status_word = nullptr;
 }  // namespace
 
+int* set_thread_status_word(int* p) {
+  int* old = t_status_word;
+  t_status_word = p;
+  return old;
+}
+
 int* device_status_ptr() {
+  if (t_status_word) return t_status_word;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev >= kMaxDev) return nullptr;
-  if (!g_status_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_device_status) != cudaSuccess) return nullptr;
-    g_status_ptr[dev] = static_cast<int*>(p);
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return nullptr;
+  int* p = g_status_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    void* q = nullptr;
+    if (cudaGetSymbolAddress(&q, g_device_status) != cudaSuccess) return nullptr;
+    p = static_cast<int*>(q);
+    g_status_ptr[dev].store(p, std::memory_order_release);
   }
-  return g_status_ptr[dev];
+  return p;
 }
 
 int num_sms() {
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= kMaxDev) return 148;
-  if (!g_nsm[dev]) {
+  if (dev < 0 || dev >= kMaxDev) return 148;
+  int v = g_nsm[dev].load(std::memory_order_relaxed);
+  if (!v) {
     int n = 0;
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    g_nsm[dev] = n > 0 ? n : 148;
+    v = n > 0 ? n : 148;
+    g_nsm[dev].store(v, std::memory_order_relaxed);
   }
-  return g_nsm[dev];
+  return v;
 }
 
 namespace {
@@ -189,6 +210,38 @@ later_status_t convert16(cudaStream_t st, int m, int n, const float* A, int64_t 
   }
   TraceScope trace(st, TRACE_OTHER);
   convert_kernel<<<grid, block, 0, st>>>(m, n, A, lda, hi, lo, ldh, prec, device_status_ptr());
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+
+namespace {
+
+// The two bounded waits the kernels use, each on something that never
+// happens: an mbarrier phase nobody arrives on (the GEMM pipeline's wait) and
+// a global flag nobody sets (the leaf's grid barrier polls a counter the same
+// way). Each gives up after `budget` cycles and reports DEV_TIMEOUT.
+__global__ void wait_selftest_kernel(int* status, long long budget) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_barrier_init();
+  if (!mbar_wait(&bar, 0, budget)) report(status, DEV_TIMEOUT);
+  const long long t0 = clock64();
+  while (*static_cast<volatile int*>(&g_never_set) == 0) {
+    if (clock64() - t0 > budget) {
+      report(status, DEV_TIMEOUT);
+      break;
+    }
+  }
+}
+
+}  // namespace
+
+later_status_t wait_selftest(cudaStream_t st, long long budget) {
+  int* status = device_status_ptr();
+  if (!status) return LATER_ERR_CUDA;
+  wait_selftest_kernel<<<1, 32, 0, st>>>(status, budget > 0 ? budget : kDefaultBudgetCycles);
   note_launch();
   return cuda_status(cudaGetLastError());
 }

@@ -29,3 +29,15 @@ def cuda():
     import later_gb300
     later_gb300.lib()
     return torch.device("cuda:0")
+
+
+@pytest.fixture(scope="session")
+def ref(cuda):
+    """The reference LATER on the GPU (oracle/_ref: its kernels + restated host code), or skip."""
+    from oracle import build_ref
+    if not build_ref.available():
+        build_ref.build()
+    r = build_ref.load()
+    if r is None:
+        pytest.skip("oracle/_ref (the reference's kernels and harness) is not built")
+    return r

@@ -95,11 +95,13 @@ def test_rtrmm(cuda, m, n):
     assert lg.device_status() == 0
     ref = np.tril(L).astype(np.float64) @ B
     err = np.linalg.norm(dC.cpu().numpy() - ref) / np.linalg.norm(ref)
-    assert err < BOUND["fp16"], err
+    err_o = np.linalg.norm(lo.rtrmm(L, B) - ref) / np.linalg.norm(ref)  # the reference's arithmetic
+    assert err < max(3 * err_o, 1e-6) and err < BOUND["fp16"], (err, err_o)
 
 
 @pytest.mark.parametrize("n,kappa,prec", [(100, 1e2, "fp16"), (1024, 1e2, "fp16"), (4096, 1e2, "fp16"),
-                                          (2000, 1e2, "bf16"), (2048, 1e6, "split3")])
+                                          (2000, 1e2, "bf16"), (2048, 1e6, "split3"), (6144, 1e2, "fp16"),
+                                          (4096, 1e4, "bf16")])
 def test_rpotrf(cuda, n, kappa, prec):
     A = gen.spd_matrix(n, kappa, seed=n)
     dA = dev(A)
@@ -107,7 +109,9 @@ def test_rpotrf(cuda, n, kappa, prec):
     assert lg.device_status() == 0
     L = np.tril(dA.cpu().numpy())
     bwd = metrics.chol_backward_error(A, L)
-    assert bwd < BOUND[prec], bwd
+    # the oracle's restatement of l_potrf (FP32 leaves up to 2048, FP16 trsm / syrk updates above)
+    bwd_o = metrics.chol_backward_error(A, lo.rpotrf(A, prec=prec))
+    assert bwd < max(3 * bwd_o, 1e-6) and bwd < BOUND[prec], (bwd, bwd_o)
     # strictly upper triangle untouched
     iu = np.triu_indices(n, 1)
     assert np.array_equal(dA.cpu().numpy()[iu], A[iu])

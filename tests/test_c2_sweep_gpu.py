@@ -1,0 +1,131 @@
+"""The QR precision sweep on the GPU: its shapes (16384 x 2048 and 65536 x 4096, which select the
+wide persistent GEMM tiles of the headline run), its SVD-constructed inputs (kappa 1e1, 1e3, 1e5) for
+rgsqrf and rhouqr in every precision mode, and the reference's own panel algorithm (panel = "mgs")
+against the oracle elementwise. Errors are FP64 (host LAPACK-level arithmetic or FP64 GPU products)."""
+import numpy as np
+import pytest
+import torch
+
+import later_gb300 as lg
+from oracle import gen, metrics
+from oracle import later_oracle as lo
+from tests.gpu_metrics import qr_errors_fp64
+
+pytestmark = pytest.mark.gpu
+
+FACTOR = 3.0
+BOUND_BWD = {"fp16": 5e-4, "bf16": 4e-3, "split3": 2e-6, "split2": 2e-6}
+
+
+def _dev(A):
+    return lg.colmajor(torch.from_numpy(np.ascontiguousarray(A)).cuda())
+
+
+def _gpu_normal(m, n, seed):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    return torch.randn(n, m, generator=g, device="cuda").t()  # column-major m x n
+
+
+def test_rgsqrf_wide_update_tiles_split2(cuda):
+    """16384 x 2048 in SPLIT2: the top-level update A2 -= Q1 R12 (16384 x 1024 x 1024) runs the
+    persistent kernel with 256-column tiles and the hi + lo split of Q1 (the headline's update kernel).
+    Checked against the oracle on the same input (FP64 metrics on the host)."""
+    m, n = 16384, 2048
+    A = gen.normal(m, n, seed=77)
+    dA = _dev(A)
+    R = lg.later_rgsqrf(dA, precision="split2")
+    assert lg.device_status() == 0
+    Q, Rc = dA.cpu().numpy(), R.cpu().numpy()
+    Qo, Ro = lo.rgsqrf(A, prec="split2")
+    bwd, orth = metrics.qr_backward_error(A, Q, Rc), metrics.orthogonality(Q)
+    bwd_o, orth_o = metrics.qr_backward_error(A, Qo, Ro), metrics.orthogonality(Qo)
+    assert bwd <= max(FACTOR * bwd_o, 1e-6) and bwd <= BOUND_BWD["split2"], (bwd, bwd_o)
+    assert orth <= max(FACTOR * orth_o, 1e-5), (orth, orth_o)
+    assert np.all(np.tril(Rc, -1) == 0) and np.all(np.diag(Rc) > 0)
+
+
+@pytest.mark.parametrize("prec,bound", [("fp16", 5e-4), ("split2", 1e-5)])
+def test_rgsqrf_tall_config_shape(cuda, prec, bound):
+    """65536 x 4096 (the sweep's tall shape): 65536-row leaves take the streaming leaf kernel, the
+    top-level products are 2048 x 2048 x 65536 and 65536 x 2048 x 2048. FP64 errors on the GPU."""
+    m, n = 65536, 4096
+    A0 = _gpu_normal(m, n, seed=5)
+    A = lg.empty_colmajor(m, n)
+    A.copy_(A0)
+    R = lg.later_rgsqrf(A, precision=prec)
+    assert lg.device_status() == 0
+    bwd, orth = qr_errors_fp64(A0, A, R)
+    assert bwd <= bound, bwd
+    assert orth <= 5e-3, orth
+    d = torch.diagonal(R)
+    assert bool((d > 0).all()) and bool((torch.tril(R, -1) == 0).all())
+
+
+def test_rgsqrf_square_headline_shape_fp64(cuda):
+    """16384^2 in SPLIT2, the benchmark's headline run: backward error below 1e-5 in FP64."""
+    m = n = 16384
+    A0 = _gpu_normal(m, n, seed=1)
+    A = lg.empty_colmajor(m, n)
+    A.copy_(A0)
+    R = lg.later_rgsqrf(A, precision="split2")
+    assert lg.device_status() == 0
+    bwd, orth = qr_errors_fp64(A0, A, R)
+    assert bwd <= 1e-5, bwd
+    assert orth / n <= 1e-3, orth
+
+
+KAPPAS = [1e1, 1e3, 1e5]
+RG_MODES = [("fp16", False), ("bf16", False), ("split3", False), ("split2", False), ("fp16", True)]
+
+
+@pytest.mark.parametrize("kappa", KAPPAS)
+@pytest.mark.parametrize("prec,cgs2", RG_MODES)
+def test_rgsqrf_kappa_sweep(cuda, kappa, prec, cgs2):
+    """SVD-constructed A = U diag(sigma) V^T, sigma geometric from 1 to 1/kappa: the GPU's FP64
+    backward error and orthogonality within 3x of the oracle's in every precision mode."""
+    A = gen.svd_matrix(4096, 1024, kappa, seed=int(np.log10(kappa)) + 30)
+    dA = _dev(A)
+    R = lg.later_rgsqrf(dA, precision=prec, cgs2=cgs2)
+    assert lg.device_status() == 0
+    Q, Rc = dA.cpu().numpy(), R.cpu().numpy()
+    Qo, Ro = lo.rgsqrf(A, prec=prec, cgs2=cgs2)
+    bwd, orth = metrics.qr_backward_error(A, Q, Rc), metrics.orthogonality(Q)
+    bwd_o, orth_o = metrics.qr_backward_error(A, Qo, Ro), metrics.orthogonality(Qo)
+    assert bwd <= max(FACTOR * bwd_o, 1e-6) and bwd <= BOUND_BWD[prec], (bwd, bwd_o)
+    assert orth <= max(FACTOR * orth_o, 1e-5), (orth, orth_o)
+
+
+@pytest.mark.parametrize("kappa", KAPPAS)
+@pytest.mark.parametrize("prec", ["fp16", "bf16", "split3"])
+def test_rhouqr_kappa_sweep(cuda, kappa, prec):
+    A = gen.svd_matrix(4096, 1024, kappa, seed=int(np.log10(kappa)) + 40)
+    dA = _dev(A)
+    W, R = lg.later_rhouqr(dA, precision=prec)
+    assert lg.device_status() == 0
+    Rc = R.cpu().numpy()
+    lg.later_ormqr(W, dA)
+    assert lg.device_status() == 0
+    Q = W.cpu().numpy()
+    Yo, Wo, Ro = lo.rhouqr(A, prec=prec)
+    Qo = lo.ormqr(Wo, Yo)
+    bwd, orth = metrics.qr_backward_error(A, Q, Rc), metrics.orthogonality(Q)
+    bwd_o, orth_o = metrics.qr_backward_error(A, Qo, Ro), metrics.orthogonality(Qo)
+    assert bwd <= max(FACTOR * bwd_o, 1e-6) and bwd <= BOUND_BWD[prec], (bwd, bwd_o)
+    assert orth <= max(FACTOR * orth_o, 2e-5), (orth, orth_o)
+
+
+@pytest.mark.parametrize("m,n,prec,tol", [(4096, 512, "split3", 2e-5), (2048, 256, "fp16", 2e-3),
+                                          (1000, 256, "split3", 2e-5)])
+def test_mgs_panels_match_oracle_elementwise(cuda, m, n, prec, tol):
+    """panel = "mgs" runs the reference's leaf algorithm (MGS-TSQR over 256-row blocks, FP32 block-CGS
+    glue) that the oracle restates: Q and R agree entry by entry, to FP32 rounding in SPLIT3 and to FP16
+    operand rounding in FP16."""
+    A = gen.normal(m, n, seed=m + 2 * n)
+    dA = _dev(A)
+    R = lg.later_rgsqrf(dA, precision=prec, panel="mgs")
+    assert lg.device_status() == 0
+    Q, Rc = dA.cpu().numpy(), R.cpu().numpy()
+    Qo, Ro = lo.rgsqrf(A, prec=prec)
+    eq = np.abs(Q - Qo).max() / np.abs(Qo).max()
+    er = np.abs(np.triu(Rc) - np.triu(Ro)).max() / np.abs(Ro).max()
+    assert eq <= tol and er <= tol, (eq, er)

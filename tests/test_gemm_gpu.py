@@ -83,3 +83,34 @@ def test_gemm_leading_dims(cuda):
     lg.gemm16("T", "N", A, B, D=D)
     ref = _ref("T", "N", A, B, 1.0, 0.0, None)
     assert (D.double() - ref).norm() / ref.norm() < rel_tol(k)
+
+
+# The shapes below make tc_gemm pick BN = 256 (tiles_m * ceil(N / 256) >= the SM count) with no split-K,
+# so they run the persistent kernels that carry the 16384^2 QR: the top-level projection R12 = Q1^T A2 (TN)
+# and the update A2 -= Q1 R12 (NN, in place, alpha = -1, beta = 1).
+@pytest.mark.parametrize("prec,dt", [("fp16", torch.float16), ("bf16", torch.bfloat16)])
+def test_gemm_persistent_bn256_projection(cuda, prec, dt):
+    m, n, k = 4096, 4096, 8192
+    g = torch.Generator(device="cuda").manual_seed(41)
+    A = _operand(k, m, dt, gen=g)
+    B = _operand(k, n, dt, gen=g)
+    work = torch.empty(1 << 24, dtype=torch.float32, device="cuda")
+    D = lg.gemm16("T", "N", A, B, precision=prec, work=work)
+    assert lg.device_status() == 0
+    ref = _ref("T", "N", A, B, 1.0, 0.0, None)
+    err = (D.double() - ref).norm() / ref.norm()
+    assert err < rel_tol(k), float(err)
+
+
+def test_gemm_persistent_bn256_update(cuda):
+    m, n, k = 16384, 2048, 2048
+    g = torch.Generator(device="cuda").manual_seed(43)
+    A = _operand(m, k, torch.float16, gen=g)
+    B = _operand(k, n, torch.float16, gen=g)
+    C = lg.colmajor(torch.randn(m, n, generator=g, device="cuda"))
+    ref = _ref("N", "N", A, B, -1.0, 1.0, C)
+    work = torch.empty(1 << 24, dtype=torch.float32, device="cuda")
+    lg.gemm16("N", "N", A, B, alpha=-1.0, beta=1.0, C=C, D=C, work=work)
+    assert lg.device_status() == 0
+    err = (C.double() - ref).norm() / ref.norm()
+    assert err < rel_tol(k), float(err)

@@ -1,10 +1,11 @@
 """Pins the CPU oracle (the numpy restatement of the reference's algorithms).
 
-The reference ships no golden vectors, so the restatement is pinned by
-mathematics the reference's outputs must satisfy: the thin QR with a positive
-diagonal is unique (rgsqrf, MGS R_kk > 0, QR/panel.cu:281-284), and the
-Householder reconstruction with the sign choice must reproduce LAPACK dgeqrf's
-reflectors and R (rhouqr). Also checks the committed fixtures in tests/golden/.
+The reference ships no golden vectors. Besides the golden vectors generated
+from the reference itself on a GPU (tests/test_golden.py), the restatement is
+pinned here by mathematics the reference's outputs must satisfy: the thin QR
+with a positive diagonal is unique (rgsqrf, MGS R_kk > 0, QR/panel.cu:281-284),
+and the Householder reconstruction with the sign choice must reproduce LAPACK
+dgeqrf's reflectors and R (rhouqr).
 """
 import numpy as np
 import pytest
