@@ -7,9 +7,12 @@
  * links against liblater_gb300.so unchanged for these calls:
  *
  *   later_rgsqrf  LATER.h:39     later_rhouqr  LATER.h:41
- *   later_ormqr   LATER.h:43     later_ormqr2  LATER.h:47
+ *   later_ormqr   LATER.h:43     later_bhouqr  LATER.h:45
+ *   later_ormqr2  LATER.h:47
  *   later_rtrsm   LATER.h:60     later_rsyrk   LATER.h:62
- *   later_rtrmm   LATER.h:64     later_rpotrf  LATER.h:80
+ *   later_rtrmm   LATER.h:64     later_qdwh_polar LATER.h:70
+ *   later_sy2sb_rec LATER.h:72   ssytrd_sy2sb  LATER.h:74
+ *   later_rpotrf  LATER.h:80
  *
  * Behaviour differences (a superset of the reference's):
  *   - errors never exit(): every call records a later_status_t, readable with
@@ -18,6 +21,20 @@
  *     has cuBLAS loaded (cublasGetStream is looked up at run time; this library
  *     does not link cuBLAS), else on the default stream;
  *   - any lda >= m is honoured; R is written in full, zeros below the diagonal;
+ *   - later_qdwh_polar reads the n x n input from tmpA (ld n) and writes U to
+ *     the top n x n block of A (lda >= n) and H to H, like the reference's
+ *     (which leaves H untouched); it symmetrises every iterate as the
+ *     reference does, so A must be symmetric; SPLIT3 + CGS2 QR, tolerance
+ *     1e-6, library-owned workspace;
+ *   - later_sy2sb_rec reduces the symmetric A (both triangles stored, lda)
+ *     to band form in place with bandwidth 128 (ns, oriA unused);
+ *     ssytrd_sy2sb reduces A_cpy in place with bandwidth nb and writes the
+ *     reflectors Y below the band into A (the reference factors its panels
+ *     from A while updating A_cpy). Both run in SPLIT3 with library-owned
+ *     workspace; n must be a multiple of the bandwidth;
+ *   - later_bhouqr runs its updates in SPLIT3 (the FP32 level of the
+ *     reference's SGEMMs) and needs more scratch than the m*n work / hwork the
+ *     reference's test passes; it uses the library-owned workspace below;
  *   - rtrsm / rsyrk / rtrmm / rpotrf, whose reference signatures carry no
  *     workspace sizes, use a library-owned workspace per (device, stream)
  *     instead of the caller's `work` / `hwork`. It grows when a larger
@@ -27,8 +44,7 @@
  *     buffers, and calls on one stream use them in stream order. The C ABI
  *     (later_c.h) takes explicit workspaces and never allocates.
  * The helper functions of the reference header (timers, generators, s2h and
- * friends, the out-of-core / EVD / blocked routines) are outside this
- * library's scope and are not declared here.
+ * friends) and the out-of-core QR routines are not declared here.
  */
 #pragma once
 
@@ -52,6 +68,9 @@ void later_rhouqr(cudaCtxt ctxt, int m, int n, float* A, int lda, float* W, int 
 
 void later_ormqr(int m, int n, float* W, int ldw, float* Y, int ldy, float* work);
 
+void later_bhouqr(int m, int n, float* A, int lda, float* W, int ldw, float* R, int ldr, float* work, int lwork,
+                  __half* hwork, int lhwork, float* U);
+
 void later_ormqr2(int m, int n, float* W, int ldw, float* Y, int ldy, float* work);
 
 void later_rtrsm(cublasHandle_t handle, char uplo, char leri, char trans, int m, int n, float* A, int lda, float* B,
@@ -63,6 +82,15 @@ void later_rsyrk(cublasHandle_t handle, int n, int k, float alpha, float* A, int
 void later_rtrmm(int m, int n, float* A, int lda, float* B, int ldb, float* C, int ldc, float* tempC, __half* hwork);
 
 void later_rpotrf(char uplo, int n, float* A, int lda, float* work, __half* hwork);
+
+void later_qdwh_polar(cudaCtxt ctxt, int n, float* A, int lda, float* H, int ldh, float* tmpA, float* work,
+                      __half* hwork);
+
+void later_sy2sb_rec(cudaCtxt ctxt, int n, int ns, float* A, float* oriA, int lda, float* work, int lwork,
+                     __half* hwork, int lhwork);
+
+void ssytrd_sy2sb(cudaCtxt ctxt, int n, int nb, float* A, float* A_cpy, int lda, float* work, int lwork,
+                  __half* hwork, int lhwork);
 
 /* Status of the last call made through this header on the calling thread. */
 later_status_t later_get_last_status();

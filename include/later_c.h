@@ -110,6 +110,70 @@ later_status_t later_c_rhouqr(later_stream_t stream, int m, int n, float* A, int
                               float* R, int ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork,
                               const later_options_t* opt);
 
+/* Minimum `work` (floats) and `hwork` (16-bit elements) for later_c_bhouqr. */
+later_status_t later_c_bhouqr_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork,
+                                      int64_t* lhwork);
+
+/*
+ * Blocked Householder QR with 128-column rhouqr panels.
+ * Replaces LATER include/LATER.h:45 later_bhouqr (QR/later_bhouqr.cu:88-189).
+ * Outputs as later_c_rhouqr: Y (unit lower trapezoidal) in A, W (m x n,
+ * ldw) with Q = I - W Y^T, R (n x n, zeros below the diagonal). The trailing
+ * updates and the W merges run on the tensor cores in opt->precision (FP16,
+ * BF16 or SPLIT3; the reference's FP32 SGEMMs correspond to SPLIT3); the
+ * 128-column panels run in FP32 as the reference's do. W's rows above each
+ * panel are zeroed before its merge. Requires m >= n and n a multiple of 32.
+ * later_c_ormqr forms Q from the result (the reference's later_ormqr2).
+ */
+later_status_t later_c_bhouqr(later_stream_t stream, int m, int n, float* A, int lda, float* W, int ldw,
+                              float* R, int ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                              const later_options_t* opt);
+
+/* Minimum `work` (floats) and `hwork` (16-bit elements) for later_c_qdwh_polar. */
+later_status_t later_c_qdwh_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork, int64_t* lhwork);
+
+/*
+ * Polar decomposition A = U H by the QR-based dynamically weighted Halley
+ * iteration (QDWH). Replaces LATER include/LATER.h:70 later_qdwh_polar
+ * (EVD/later_qdwh_polar.cu:24-110), which runs later_rgsqrf on the
+ * (m + n) x n stack [sqrt(c) X; I] and one tensor-core product per step.
+ * A (m x n, m >= n, n a multiple of 32) is read only; U (m x n, ldu) receives
+ * the polar factor with orthonormal columns, H (n x n, ldh; may be NULL) the
+ * symmetric positive semidefinite factor. The stack's QR runs with CGS2 and
+ * opt->precision (FP16 / BF16 / SPLIT3; SPLIT2 is taken as SPLIT3): Q must be
+ * orthonormal to working accuracy although the stack's condition number is
+ * about sqrt(c), so SPLIT3 is needed for an FP32-level U. l0 > 0 is a lower
+ * bound on the smallest singular value of A / ||A||_F (0: estimated as
+ * 1 / ||R0^{-1}||_F from a QR of it); `symmetric` symmetrises every iterate
+ * (square symmetric A only, as the reference does); tol (0: 1e-6) sets the
+ * stopping test 1 - l < 5 tol, ||X_k+1 - X_k||_F < (5 tol)^(1/3); max_iter (0:
+ * 10). *iterations (may be NULL) receives the number of steps taken. Host
+ * code reads two norms per step, so the call synchronises the stream.
+ */
+later_status_t later_c_qdwh_polar(later_stream_t stream, int m, int n, const float* A, int lda, float* U, int ldu,
+                                  float* H, int ldh, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                                  const later_options_t* opt, double l0, int symmetric, double tol, int max_iter,
+                                  int* iterations);
+
+/* Minimum `work` (floats) and `hwork` (16-bit elements) for later_c_sy2sb. */
+later_status_t later_c_sy2sb_bufsize(int n, int nb, const later_options_t* opt, int64_t* lwork, int64_t* lhwork);
+
+/*
+ * Symmetric to band reduction B = Q^T A Q with bandwidth nb (32, 64, 96 or
+ * 128; n a multiple of nb). Replaces LATER include/LATER.h:72-74
+ * later_sy2sb_rec / ssytrd_sy2sb (EVD/later_sy2sb_rec.cu,
+ * EVD/later_sy2sb_blocked.cu:23-186): rhouqr panels and the two-sided ZY
+ * update A22 -= Y Z^T + Z Y^T, Z = A22 W - Y (W^T A22 W) / 2, on the tensor
+ * cores in opt->precision (FP16 / BF16 / SPLIT3). A (n x n, both triangles
+ * stored) is overwritten by B in the same full storage, zeros outside the
+ * band. Y and W (n x n each, may be NULL) receive the reflectors of block
+ * column i in rows i+nb.. of columns i..i+nb-1 (zeros elsewhere), so that
+ * Q = prod_i (I - W_i Y_i^T).
+ */
+later_status_t later_c_sy2sb(later_stream_t stream, int n, int nb, float* A, int lda, float* Y, int ldy, float* W,
+                             int ldw, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                             const later_options_t* opt);
+
 /*
  * Explicit Q = I - W Y^T (first n columns), written over W, in FP32.
  * Replaces LATER include/LATER.h:43 later_ormqr and :47 later_ormqr2

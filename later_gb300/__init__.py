@@ -19,7 +19,9 @@ from . import build as _build
 
 __all__ = [
     "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
-    "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "later_rsyrk", "later_rtrsm",
+    "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "later_bhouqr",
+    "bhouqr_bufsize", "later_ormqr2", "later_qdwh_polar", "qdwh_bufsize", "later_sy2sb",
+    "sy2sb_bufsize", "later_rsyrk", "later_rtrsm",
     "later_rtrmm", "later_rpotrf", "blas3_bufsize",
     "spd_solve", "ls_solve", "BatchedQR", "LsServer", "gemm16", "convert16", "device_status", "wait_selftest", "launch_count", "trace_begin",
     "trace_end",
@@ -99,6 +101,14 @@ _SIGS = {
     "later_c_rhouqr_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "later_c_rhouqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_ormqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i64]),
+    "later_c_sy2sb_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "later_c_sy2sb": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
+    "later_c_qdwh_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "later_c_qdwh_polar": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64,
+                                ctypes.POINTER(Options), ctypes.c_double, _i, ctypes.c_double, _i,
+                                ctypes.POINTER(_i)]),
+    "later_c_bhouqr_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
+    "later_c_bhouqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_blas3_bufsize": (_i, [ctypes.c_char, ctypes.c_char, _i, _i, ctypes.POINTER(Options),
                                    ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "later_c_rsyrk": (_i, [_vp, _i, _i, _f, _vp, _i, _f, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
@@ -262,6 +272,109 @@ def later_rhouqr(A, W=None, R=None, work=None, hwork=None, *, precision="fp16", 
                                 R.data_ptr(), _ld(R, "R"), work.data_ptr(), work.numel(), hwork.data_ptr(),
                                 hwork.numel(), ctypes.byref(o)), "later_rhouqr")
     return W, R
+
+
+def bhouqr_bufsize(m, n, precision="fp16"):
+    o = Options.make(precision)
+    lw, lh = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().later_c_bhouqr_bufsize(m, n, ctypes.byref(o), ctypes.byref(lw), ctypes.byref(lh)), "bhouqr_bufsize")
+    return lw.value, lh.value
+
+
+def later_bhouqr(A, W=None, R=None, work=None, hwork=None, *, precision="split3", timeout_cycles=0, stream=None):
+    """Blocked Householder QR over 128-column rhouqr panels: A becomes Y; returns (W, R), Q = I - W Y^T.
+
+    Mirrors LATER's `later_bhouqr(m, n, A, lda, W, ldw, R, ldr, work, lwork, hwork, lhwork, U)`
+    (include/LATER.h:45); the reference's FP32 updates correspond to precision "split3".
+    """
+    import torch
+    m, n = A.shape
+    if W is None:
+        W = empty_colmajor(m, n, device=A.device)
+    if R is None:
+        R = empty_colmajor(n, n, device=A.device)
+    lw, lh = bhouqr_bufsize(m, n, precision)
+    if work is None:
+        work = torch.empty(lw, dtype=torch.float32, device=A.device)
+    if hwork is None:
+        hwork = torch.empty(lh, dtype=torch.float16, device=A.device)
+    o = Options.make(precision, False, 128, timeout_cycles)
+    _check(lib().later_c_bhouqr(_stream(stream), m, n, A.data_ptr(), _ld(A, "A"), W.data_ptr(), _ld(W, "W"),
+                                R.data_ptr(), _ld(R, "R"), work.data_ptr(), work.numel(), hwork.data_ptr(),
+                                hwork.numel(), ctypes.byref(o)), "later_bhouqr")
+    return W, R
+
+
+def qdwh_bufsize(m, n, precision="split3"):
+    o = Options.make(precision)
+    lw, lh = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().later_c_qdwh_bufsize(m, n, ctypes.byref(o), ctypes.byref(lw), ctypes.byref(lh)), "qdwh_bufsize")
+    return lw.value, lh.value
+
+
+def later_qdwh_polar(A, U=None, H=None, *, precision="split3", l0=0.0, symmetric=False, tol=1e-6, max_iter=10,
+                     work=None, hwork=None, stream=None):
+    """Polar decomposition A = U H by QDWH; returns (U, H, iterations).
+
+    Mirrors LATER's `later_qdwh_polar(ctxt, n, A, lda, H, ldh, tmpA, work, hwork)` (include/LATER.h:70) with
+    the input A (m x n, m >= n) read only; see later_c.h for the options.
+    """
+    import torch
+    m, n = A.shape
+    if U is None:
+        U = empty_colmajor(m, n, device=A.device)
+    if H is None:
+        H = empty_colmajor(n, n, device=A.device)
+    lw, lh = qdwh_bufsize(m, n, precision)
+    if work is None:
+        work = torch.empty(lw, dtype=torch.float32, device=A.device)
+    if hwork is None:
+        hwork = torch.empty(lh, dtype=torch.float16, device=A.device)
+    o = Options.make(precision)
+    it = ctypes.c_int(0)
+    _check(lib().later_c_qdwh_polar(_stream(stream), m, n, A.data_ptr(), _ld(A, "A"), U.data_ptr(), _ld(U, "U"),
+                                    H.data_ptr(), _ld(H, "H"), work.data_ptr(), work.numel(), hwork.data_ptr(),
+                                    hwork.numel(), ctypes.byref(o), float(l0), int(bool(symmetric)), float(tol),
+                                    int(max_iter), ctypes.byref(it)), "later_qdwh_polar")
+    return U, H, it.value
+
+
+def sy2sb_bufsize(n, nb=128, precision="split3"):
+    o = Options.make(precision)
+    lw, lh = ctypes.c_int64(), ctypes.c_int64()
+    _check(lib().later_c_sy2sb_bufsize(n, nb, ctypes.byref(o), ctypes.byref(lw), ctypes.byref(lh)), "sy2sb_bufsize")
+    return lw.value, lh.value
+
+
+def later_sy2sb(A, nb=128, *, precision="split3", Y=None, W=None, reflectors=True, work=None, hwork=None,
+                stream=None):
+    """Symmetric to band reduction in place: A (n x n, both triangles) becomes B = Q^T A Q with bandwidth nb.
+    Returns (Y, W) with Q = prod_i (I - W_i Y_i^T) per block column (None, None without reflectors).
+
+    Mirrors LATER's `ssytrd_sy2sb` / `later_sy2sb_rec` (include/LATER.h:72-74).
+    """
+    import torch
+    n = A.shape[0]
+    if reflectors:
+        Y = Y if Y is not None else empty_colmajor(n, n, device=A.device)
+        W = W if W is not None else empty_colmajor(n, n, device=A.device)
+    lw, lh = sy2sb_bufsize(n, nb, precision)
+    if work is None:
+        work = torch.empty(lw, dtype=torch.float32, device=A.device)
+    if hwork is None:
+        hwork = torch.empty(lh, dtype=torch.float16, device=A.device)
+    o = Options.make(precision)
+    _check(lib().later_c_sy2sb(_stream(stream), n, nb, A.data_ptr(), _ld(A, "A"),
+                               Y.data_ptr() if Y is not None else None, _ld(Y, "Y") if Y is not None else n,
+                               W.data_ptr() if W is not None else None, _ld(W, "W") if W is not None else n,
+                               work.data_ptr(), work.numel(), hwork.data_ptr(), hwork.numel(), ctypes.byref(o)),
+           "later_sy2sb")
+    return Y, W
+
+
+def later_ormqr2(W, Y, work=None, stream=None):
+    """Explicit Q = I - W Y^T from later_bhouqr's output, written over W (include/LATER.h:47)."""
+    return later_ormqr(W, Y, work=work, stream=stream)
 
 
 def later_ormqr(W, Y, work=None, stream=None):

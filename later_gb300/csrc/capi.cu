@@ -76,6 +76,52 @@ later_status_t later_c_rhouqr_bufsize(int m, int n, const later_options_t* opt, 
   return LATER_OK;
 }
 
+later_status_t later_c_bhouqr_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork, int64_t* lhwork) {
+  if (m < 1 || n < 1 || m < n) return LATER_ERR_INVALID_ARG;
+  const QrNeed q = bhouqr_need(m, n, options_from(opt));
+  if (lwork) *lwork = q.rec_work;
+  if (lhwork) *lhwork = q.hwork;
+  return LATER_OK;
+}
+
+later_status_t later_c_bhouqr(later_stream_t stream, int m, int n, float* A, int lda, float* W, int ldw, float* R,
+                              int ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                              const later_options_t* opt) {
+  return bhouqr(reinterpret_cast<cudaStream_t>(stream), m, n, A, lda, W, ldw, R, ldr, work, lwork, hwork, lhwork,
+                options_from(opt));
+}
+
+later_status_t later_c_qdwh_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork, int64_t* lhwork) {
+  if (m < 1 || n < 1 || m < n) return LATER_ERR_INVALID_ARG;
+  const QrNeed q = qdwh_need(m, n, options_from(opt));
+  if (lwork) *lwork = q.rec_work;
+  if (lhwork) *lhwork = q.hwork;
+  return LATER_OK;
+}
+
+later_status_t later_c_qdwh_polar(later_stream_t stream, int m, int n, const float* A, int lda, float* U, int ldu,
+                                  float* H, int ldh, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                                  const later_options_t* opt, double l0, int symmetric, double tol, int max_iter,
+                                  int* iterations) {
+  return qdwh_polar(reinterpret_cast<cudaStream_t>(stream), m, n, A, lda, U, ldu, H, ldh, work, lwork, hwork, lhwork,
+                    options_from(opt), l0, symmetric, tol, max_iter, iterations);
+}
+
+later_status_t later_c_sy2sb_bufsize(int n, int nb, const later_options_t* opt, int64_t* lwork, int64_t* lhwork) {
+  if (n < 1 || nb < 1) return LATER_ERR_INVALID_ARG;
+  const QrNeed q = sy2sb_need(n, nb, options_from(opt));
+  if (lwork) *lwork = q.rec_work;
+  if (lhwork) *lhwork = q.hwork;
+  return LATER_OK;
+}
+
+later_status_t later_c_sy2sb(later_stream_t stream, int n, int nb, float* A, int lda, float* Y, int ldy, float* W,
+                             int ldw, float* work, int64_t lwork, void* hwork, int64_t lhwork,
+                             const later_options_t* opt) {
+  return sy2sb(reinterpret_cast<cudaStream_t>(stream), n, nb, A, lda, Y, ldy, W, ldw, work, lwork, hwork, lhwork,
+               options_from(opt));
+}
+
 later_status_t later_c_rhouqr(later_stream_t stream, int m, int n, float* A, int lda, float* W, int ldw, float* R,
                               int ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork,
                               const later_options_t* opt) {

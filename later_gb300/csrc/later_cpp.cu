@@ -34,7 +34,7 @@ cudaStream_t stream_of(cublasHandle_t h) {
 }
 
 // Library-owned workspace for the routines whose reference signatures carry
-// no workspace (rtrsm, rsyrk, rtrmm, rpotrf): one float and one 16-bit buffer
+// no workspace (rtrsm, rsyrk, rtrmm, rpotrf) or too little (bhouqr): one float and one 16-bit buffer
 // per (device, stream), grown to the largest request seen on that stream and
 // kept until exit. A call holds the cache lock from the lookup until its work
 // is enqueued, so each buffer is used in its stream's order only: calls on
@@ -101,6 +101,46 @@ void later_rhouqr(cudaCtxt ctxt, int m, int n, float* A, int lda, float* W, int 
 void later_ormqr(int m, int n, float* W, int ldw, float* Y, int ldy, float* work) {
   // The caller's work holds m*n floats (QR/later_ormqr.cu:48 allocated that much itself).
   record("later_ormqr", ormqr(nullptr, m, n, W, ldw, Y, ldy, work, static_cast<int64_t>(m) * n));
+}
+
+void later_bhouqr(int m, int n, float* A, int lda, float* W, int ldw, float* R, int ldr, float*, int, __half*, int,
+                  float* /*U: not needed*/) {
+  Options o;
+  o.prec = LATER_PREC_SPLIT3;  // the reference's updates are FP32 SGEMMs (QR/later_bhouqr.cu:122-165)
+  const QrNeed q = bhouqr_need(m, n, o);
+  record("later_bhouqr", with_workspace(nullptr, q.rec_work, q.hwork, [&](float* w, int64_t lw, void* h, int64_t lh) {
+           return bhouqr(nullptr, m, n, A, lda, W, ldw, R, ldr, w, lw, h, lh, o);
+         }));
+}
+
+void later_qdwh_polar(cudaCtxt ctxt, int n, float* A, int lda, float* H, int ldh, float* tmpA, float*, __half*) {
+  Options o;
+  o.prec = LATER_PREC_SPLIT3;
+  cudaStream_t st = stream_of(ctxt.cublas_handle);
+  const QrNeed q = qdwh_need(n, n, o);
+  record("later_qdwh_polar", with_workspace(st, q.rec_work, q.hwork, [&](float* w, int64_t lw, void* h, int64_t lh) {
+           return qdwh_polar(st, n, n, tmpA, n, A, lda, H, ldh, w, lw, h, lh, o, 0.0, 1, 1e-6, 10, nullptr);
+         }));
+}
+
+void later_sy2sb_rec(cudaCtxt ctxt, int n, int /*ns*/, float* A, float* /*oriA*/, int lda, float*, int, __half*, int) {
+  Options o;
+  o.prec = LATER_PREC_SPLIT3;
+  cudaStream_t st = stream_of(ctxt.cublas_handle);
+  const QrNeed q = sy2sb_need(n, 128, o);
+  record("later_sy2sb_rec", with_workspace(st, q.rec_work, q.hwork, [&](float* w, int64_t lw, void* h, int64_t lh) {
+           return sy2sb(st, n, 128, A, lda, nullptr, 0, nullptr, 0, w, lw, h, lh, o);
+         }));
+}
+
+void ssytrd_sy2sb(cudaCtxt ctxt, int n, int nb, float* A, float* A_cpy, int lda, float*, int, __half*, int) {
+  Options o;
+  o.prec = LATER_PREC_SPLIT3;
+  cudaStream_t st = stream_of(ctxt.cublas_handle);
+  const QrNeed q = sy2sb_need(n, nb, o);
+  record("ssytrd_sy2sb", with_workspace(st, q.rec_work, q.hwork, [&](float* w, int64_t lw, void* h, int64_t lh) {
+           return sy2sb(st, n, nb, A_cpy, lda, A, lda, nullptr, 0, w, lw, h, lh, o);
+         }));
 }
 
 void later_ormqr2(int m, int n, float* W, int ldw, float* Y, int ldy, float* work) {

@@ -478,4 +478,180 @@ later_status_t ormqr(cudaStream_t st, int m, int n, float* W, int64_t ldw, const
   return copy2d(st, m, n, work, m, W, ldw);
 }
 
+
+// ======================================================================
+// Blocked Householder QR (QR/later_bhouqr.cu:88-189): for each block of
+// nb = 128 columns starting at column i,
+//   panel:   rhouqr of A[i:, i:i+nb] -> Y_i (in A), local W_i, R_ii
+//   update:  T = W_i^T A2, A2 -= Y_i T       (A2 = A[i:, i+nb:])
+//            R[i:i+nb, i+nb:] <- A2's top rows, zeroed in A
+//   merge:   W_i -= W[:, :i] (Y[:, :i]^T W_i)  (so that Q = I - W Y^T overall)
+// The reference runs the update and the merge as FP32 SGEMMs; here they are
+// tensor-core GEMMs in the requested precision (SPLIT3 = hi + lo operands,
+// three products, FP32-level accuracy; the C++ drop-in uses it). Each GEMM
+// reads 16-bit copies kept by their producers: the update's epilogue writes
+// A2's copy, the merge's epilogue writes W_i's; Y_i's and the local W_i's are
+// converted once after the panel. W_i's rows above i are zeroed before the
+// merge (the reference leaves them as the caller's memory held them).
+namespace {
+
+constexpr int kBlockNb = 128;  // QR/later_bhouqr.cu:12 NMIN
+
+struct BLayout {
+  int* counters;
+  float* T;    // nb x n   (W_i^T A2)
+  float* T2;   // n x nb   (Y[:, :i]^T W_i)
+  int64_t ldt, ldt2;
+  char* th;    // 16-bit copies of T / T2 (hi, lo)
+  char* tl;
+  char* t2h;
+  char* t2l;
+  char* ah;    // 16-bit copy of A (Y columns left of the panel, A2 right of it)
+  char* al;
+  char* wh;    // 16-bit copy of W
+  char* wl;
+  int64_t ldh;
+  float* sub_work;  // the panel's rhouqr workspace
+  int64_t sub_lwork;
+  void* sub_hwork;
+  int64_t sub_lhwork;
+};
+
+Options panel_options(const Options& o) {
+  Options p = o;
+  p.prec = LATER_PREC_FP16;  // a 128-column panel's own updates run in FP32 (n/2 <= 128, :83)
+  return p;
+}
+
+bool carve_bhou(Arena& fw, Arena& hw, int m, int n, const Options& o, BLayout* L) {
+  const bool split3 = o.prec == LATER_PREC_SPLIT3;
+  const QrNeed sub = rhouqr_need(m, std::min(n, kBlockNb), panel_options(o));
+  L->counters = fw.take<int>(kCounters);
+  L->ldt = round_up(kBlockNb, 8);
+  L->ldt2 = round_up(n, 8);
+  L->T = fw.take<float>(L->ldt * n);
+  L->T2 = fw.take<float>(L->ldt2 * kBlockNb);
+  L->sub_lwork = sub.rec_work;
+  L->sub_work = fw.take<float>(sub.rec_work);
+  L->ldh = round_up(m, 8);
+  L->ah = reinterpret_cast<char*>(hw.take<uint16_t>(L->ldh * n));
+  L->al = split3 ? reinterpret_cast<char*>(hw.take<uint16_t>(L->ldh * n)) : nullptr;
+  L->wh = reinterpret_cast<char*>(hw.take<uint16_t>(L->ldh * n));
+  L->wl = split3 ? reinterpret_cast<char*>(hw.take<uint16_t>(L->ldh * n)) : nullptr;
+  L->th = reinterpret_cast<char*>(hw.take<uint16_t>(L->ldt * n));
+  L->tl = split3 ? reinterpret_cast<char*>(hw.take<uint16_t>(L->ldt * n)) : nullptr;
+  L->t2h = reinterpret_cast<char*>(hw.take<uint16_t>(L->ldt2 * kBlockNb));
+  L->t2l = split3 ? reinterpret_cast<char*>(hw.take<uint16_t>(L->ldt2 * kBlockNb)) : nullptr;
+  L->sub_lhwork = sub.hwork;
+  L->sub_hwork = hw.take<uint16_t>(sub.hwork);
+  return !fw.failed() && !hw.failed();
+}
+
+// D (M x N) = alpha op(A) B + beta C through the tensor cores, FP32 out plus
+// its 16-bit copy (dh / dl).
+later_status_t bh_gemm(cudaStream_t st, const Options& o, int* counters, Arena& fw, char ta, int M, int N, int K,
+                       float alpha, const char* ah, const char* al, int64_t lda16, const char* bh, const char* bl,
+                       int64_t ldb16, float beta, float* D, int64_t ldd, char* dh, char* dl, int64_t ldh16) {
+  Scratch sc;
+  sc.counters = counters + 2048;
+  sc.n_counters = 2048;
+  const int64_t avail = static_cast<int64_t>(fw.remaining() / sizeof(float)) - 64;
+  sc.partial_floats = std::max<int64_t>(0, std::min<int64_t>(avail, static_cast<int64_t>(num_sms()) * 128 * 256 * 2));
+  sc.partial = sc.partial_floats > 0 ? reinterpret_cast<float*>(
+                                           (reinterpret_cast<uintptr_t>(fw.cursor()) + 255) & ~uintptr_t(255))
+                                     : nullptr;
+  if (sc.partial_floats > 0) sc.partial_floats -= 64;
+  GemmCall g;
+  g.ta = ta;
+  g.tb = 'N';
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.A = Op16{ah, al, lda16};
+  g.B = Op16{bh, bl, ldb16};
+  g.alpha = alpha;
+  g.beta = beta;
+  g.out.C = D;
+  g.out.ldc = ldd;
+  g.out.D = D;
+  g.out.ldd = ldd;
+  g.out.Dh = dh;
+  g.out.Dl = dl;
+  g.out.ldh = ldh16;
+  g.prec = o.prec;
+  g.out_prec = o.prec;
+  return tc_gemm(g, sc, st, o.budget);
+}
+
+}  // namespace
+
+QrNeed bhouqr_need(int m, int n, const Options& o) {
+  Arena fw(nullptr, 0), hw(nullptr, 0);
+  BLayout L;
+  carve_bhou(fw, hw, m, n, o, &L);
+  QrNeed q;
+  const int64_t splitk = static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 128;
+  q.min_work = static_cast<int64_t>(fw.peak() / sizeof(float)) + 64;
+  q.rec_work = q.min_work + splitk;
+  q.hwork = static_cast<int64_t>(hw.peak() / 2) + 128;
+  return q;
+}
+
+later_status_t bhouqr(cudaStream_t st, int m, int n, float* A, int64_t lda, float* W, int64_t ldw, float* R,
+                      int64_t ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
+  if (m < 1 || n < 1 || m < n || lda < m || ldw < m || ldr < n || !A || !W || !R) return LATER_ERR_INVALID_ARG;
+  if (n % 32 != 0) return LATER_ERR_INVALID_ARG;
+  if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT3) return LATER_ERR_INVALID_ARG;
+  const QrNeed need = bhouqr_need(m, n, o);
+  if (!work || !hwork || lwork < need.min_work || lhwork < need.hwork) return LATER_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(hwork) & 15) != 0) return LATER_ERR_INVALID_ARG;
+  Arena fw(work, static_cast<size_t>(lwork) * sizeof(float));
+  Arena hw(hwork, static_cast<size_t>(lhwork) * 2);
+  BLayout L;
+  if (!carve_bhou(fw, hw, m, n, o, &L)) return LATER_ERR_WORKSPACE;
+  const int64_t ldh = L.ldh;
+  auto at = [ldh](char* base, int64_t r, int64_t c) { return base ? base + (r + c * ldh) * 2 : nullptr; };
+  const Options po = panel_options(o);
+  LATER_CHECK_CUDA(cudaMemsetAsync(L.counters, 0, kCounters * sizeof(int), st));
+  LATER_CHECK(fill_strict_lower(st, n, n, R, ldr, 0.f));
+  // A2's 16-bit copy for the first update (later ones are written by the update's epilogue).
+  if (n > kBlockNb)
+    LATER_CHECK(convert16(st, m, n - kBlockNb, A + kBlockNb * lda, lda, at(L.ah, 0, kBlockNb),
+                          at(L.al, 0, kBlockNb), ldh, o.prec));
+  for (int i = 0; i < n; i += kBlockNb) {
+    const int nb = std::min(kBlockNb, n - i), mr = m - i, rest = n - i - nb;
+    float* Ai = A + i + static_cast<int64_t>(i) * lda;
+    float* Wi = W + static_cast<int64_t>(i) * ldw;  // column block i, from row 0
+    LATER_CHECK(rhouqr(st, mr, nb, Ai, lda, Wi + i, ldw, R + i + static_cast<int64_t>(i) * ldr, ldr, L.sub_work,
+                       L.sub_lwork, L.sub_hwork, L.sub_lhwork, po));
+    // 16-bit copies of Y_i and the local W_i, zero above row i (so are W_i's FP32 rows)
+    LATER_CHECK(convert16(st, mr, nb, Ai, lda, at(L.ah, i, i), at(L.al, i, i), ldh, o.prec));
+    LATER_CHECK(convert16(st, mr, nb, Wi + i, ldw, at(L.wh, i, i), at(L.wl, i, i), ldh, o.prec));
+    if (i > 0) {
+      LATER_CHECK(zero_block(st, i, nb, nullptr, 0, at(L.ah, 0, i), at(L.al, 0, i), ldh));
+      LATER_CHECK(zero_block(st, i, nb, Wi, ldw, at(L.wh, 0, i), at(L.wl, 0, i), ldh));
+    }
+    if (rest > 0) {
+      float* A2 = A + i + static_cast<int64_t>(i + nb) * lda;
+      // T = W_i^T A2   (nb x rest, K = mr)
+      LATER_CHECK(bh_gemm(st, o, L.counters, fw, 'T', nb, rest, mr, 1.f, at(L.wh, i, i), at(L.wl, i, i), ldh,
+                          at(L.ah, i, i + nb), at(L.al, i, i + nb), ldh, 0.f, L.T, L.ldt, L.th, L.tl, L.ldt));
+      // A2 -= Y_i T   (mr x rest, K = nb), refreshing A2's 16-bit copy
+      LATER_CHECK(bh_gemm(st, o, L.counters, fw, 'N', mr, rest, nb, -1.f, at(L.ah, i, i), at(L.al, i, i), ldh, L.th,
+                          L.tl, L.ldt, 1.f, A2, lda, at(L.ah, i, i + nb), at(L.al, i, i + nb), ldh));
+      LATER_CHECK(copy2d(st, nb, rest, A2, lda, R + i + static_cast<int64_t>(i + nb) * ldr, ldr));
+      LATER_CHECK(zero_block(st, nb, rest, A2, lda, at(L.ah, i, i + nb), at(L.al, i, i + nb), ldh));
+    }
+    if (i > 0) {
+      // T2 = Y[:, :i]^T W_i   (i x nb, K = m)
+      LATER_CHECK(bh_gemm(st, o, L.counters, fw, 'T', i, nb, m, 1.f, L.ah, L.al, ldh, at(L.wh, 0, i),
+                          at(L.wl, 0, i), ldh, 0.f, L.T2, L.ldt2, L.t2h, L.t2l, L.ldt2));
+      // W_i -= W[:, :i] T2   (m x nb, K = i), refreshing W_i's 16-bit copy
+      LATER_CHECK(bh_gemm(st, o, L.counters, fw, 'N', m, nb, i, -1.f, L.wh, L.wl, ldh, L.t2h, L.t2l, L.ldt2, 1.f,
+                          Wi, ldw, at(L.wh, 0, i), at(L.wl, 0, i), ldh));
+    }
+  }
+  return LATER_OK;
+}
+
 }  // namespace later

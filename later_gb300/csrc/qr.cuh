@@ -33,6 +33,22 @@ QrNeed rhouqr_need(int m, int n, const Options& o);
 later_status_t rhouqr(cudaStream_t st, int m, int n, float* A, int64_t lda, float* W, int64_t ldw, float* R,
                       int64_t ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
 
+// Blocked Householder QR over 128-column rhouqr panels (QR/later_bhouqr.cu:88-189).
+QrNeed bhouqr_need(int m, int n, const Options& o);
+later_status_t bhouqr(cudaStream_t st, int m, int n, float* A, int64_t lda, float* W, int64_t ldw, float* R,
+                      int64_t ldr, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
+
+// QDWH polar decomposition A = U H (EVD/later_qdwh_polar.cu:24-110), qdwh.cu.
+QrNeed qdwh_need(int m, int n, const Options& o);
+later_status_t qdwh_polar(cudaStream_t st, int m, int n, const float* A, int64_t lda, float* U, int64_t ldu, float* H,
+                          int64_t ldh, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o,
+                          double l0, int symmetrize, double tol, int max_iter, int* iterations);
+
+// Symmetric to band reduction B = Q^T A Q, bandwidth nb (sy2sb.cu).
+QrNeed sy2sb_need(int n, int nb, const Options& o);
+later_status_t sy2sb(cudaStream_t st, int n, int nb, float* A, int64_t lda, float* Y, int64_t ldy, float* W,
+                     int64_t ldw, float* work, int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
+
 // Q = I - W Y^T (first n columns) written over W; `work` holds m x n floats.
 later_status_t ormqr(cudaStream_t st, int m, int n, float* W, int64_t ldw, const float* Y, int64_t ldy, float* work,
                      int64_t lwork);

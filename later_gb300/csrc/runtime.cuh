@@ -100,7 +100,7 @@ later_status_t convert16(cudaStream_t st, int m, int n, const float* A, int64_t 
 later_status_t fill_strict_lower(cudaStream_t st, int m, int n, float* A, int64_t lda, float v);
 // Y += alpha X  (m x n blocks).
 later_status_t axpy2d(cudaStream_t st, int m, int n, float alpha, const float* X, int64_t ldx, float* Y, int64_t ldy);
-// X = 0 (m x n block) and the same block of its 16-bit copies (may be null).
+// X = 0 (m x n block) and the same block of its 16-bit copies (each may be null).
 later_status_t zero_block(cudaStream_t st, int m, int n, float* X, int64_t ldx, void* xh, void* xl, int64_t ldh);
 // Y = X (m x n blocks).
 later_status_t copy2d(cudaStream_t st, int m, int n, const float* X, int64_t ldx, float* Y, int64_t ldy);

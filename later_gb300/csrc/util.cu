@@ -145,7 +145,7 @@ __global__ void zero_block_kernel(int m, int n, float* X, int64_t ldx, uint16_t*
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   for (int j = blockIdx.y; j < n; j += gridDim.y) {
-    X[i + static_cast<int64_t>(j) * ldx] = 0.f;
+    if (X) X[i + static_cast<int64_t>(j) * ldx] = 0.f;
     if (xh) xh[i + static_cast<int64_t>(j) * ldh] = 0;
     if (xl) xl[i + static_cast<int64_t>(j) * ldh] = 0;
   }

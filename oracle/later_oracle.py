@@ -242,6 +242,42 @@ def rhouqr(A: np.ndarray, prec: str = "fp16", signs: bool = True):
     return a, w, r
 
 
+def bhouqr(A: np.ndarray, prec: str = "fp32", nb: int = 128, signs: bool = True):
+    """Blocked Householder QR — later_bhouqr, QR/later_bhouqr.cu:88-189.
+
+    For each block of nb columns at column i: rhouqr of A[i:, i:i+nb] (its own
+    updates in FP32 at nb = 128), the trailing update A2 -= Y_i (W_i^T A2)
+    (cublasSgemm, :117-136), R12 taken from A2's top rows and zeroed
+    (copyAndClear, :138-140), then the W merge W_i -= W[:, :i] (Y[:, :i]^T W_i)
+    (:143-165) over full-height columns whose rows above i are zero.
+    prec "fp32" is the reference's arithmetic; "fp16" / "bf16" / "split3" model
+    the same GEMMs on 16-bit operands.
+    """
+    a = np.array(A, dtype=F32, order="F")
+    m, n = a.shape
+    w = np.zeros((m, n), dtype=F32)
+    r = np.zeros((n, n), dtype=F32)
+
+    def gemm(x, y):
+        return (x @ y).astype(F32) if prec == "fp32" else tc_gemm(x, y, prec)
+
+    for i in range(0, n, nb):
+        b = min(nb, n - i)
+        y, wi, ri = rhouqr(a[i:, i:i + b], prec="fp16", signs=signs)
+        a[i:, i:i + b] = y
+        w[i:, i:i + b] = wi
+        r[i:i + b, i:i + b] = ri
+        if n - i > b:
+            t = gemm(w[i:, i:i + b].T, a[i:, i + b:])
+            a[i:, i + b:] -= gemm(a[i:, i:i + b], t)
+            r[i:i + b, i + b:] = a[i:i + b, i + b:]
+            a[i:i + b, i + b:] = 0
+        if i > 0:
+            t2 = gemm(a[:, :i].T, w[:, i:i + b])
+            w[:, i:i + b] -= gemm(w[:, :i], t2)
+    return a, w, r
+
+
 def ormqr(W: np.ndarray, Y: np.ndarray) -> np.ndarray:
     """Q = I - W Y1^T (first n columns) — QR/later_ormqr.cu:50-58, in FP32."""
     m, n = W.shape
@@ -342,3 +378,94 @@ def rpotrf(A, prec="fp16", leaf=2048):
 
     rec(a)
     return np.tril(a)
+
+
+# ---------------------------------------------------------------- QDWH polar
+def qdwh_coeffs(l: float):
+    """Dynamically weighted Halley coefficients (a, b, c) and the next lower bound, as
+    EVD/later_qdwh_polar.cu:58-65 computes them (Nakatsukasa, Bai and Gygi, SIAM J. Matrix
+    Anal. Appl. 31(5), 2010, eqs. (3.3)-(3.4))."""
+    l2 = l * l
+    dd = (4.0 * (1.0 - l2) / (l2 * l2)) ** (1.0 / 3.0)
+    sqd = np.sqrt(1.0 + dd)
+    a = sqd + np.sqrt(8.0 - 4.0 * dd + 8.0 * (2.0 - l2) / (l2 * sqd)) / 2.0
+    b = (a - 1.0) ** 2 / 4.0
+    c = a + b - 1.0
+    return a, b, c, l * (a + b * l2) / (1.0 + c * l2)
+
+
+def qdwh_polar(A: np.ndarray, prec: str = "split3", l0: float | None = None, symmetrize: bool = False,
+               tol: float = 1e-6, max_iter: int = 10):
+    """Polar decomposition A = U H by the QR-based QDWH iteration — later_qdwh_polar,
+    EVD/later_qdwh_polar.cu:24-110:
+      X0 = A / ||A||_F;  while not converged:
+        [sqrt(c) X; I] = [Q1; Q2] R   (rgsqrf of the (m + n) x n stack)
+        X <- (b/c) X + (a - b/c)/sqrt(c) Q1 Q2^T
+    stopping when 1 - l < 10 eps and ||X_new - X||_F < (10 eps)^(1/3) (the reference's tol1 / tol3,
+    with its eps = 2e-4 replaced by `tol`). H = (U^T A + (U^T A)^T) / 2. l0 defaults to
+    1 / ||R0^{-1}||_F for X0 = Q0 R0, a guaranteed lower bound on sigma_min(X0).
+    The stack's QR must be orthonormal to working accuracy although its condition number is about
+    sqrt(c) (1e4 in the first step at kappa 1e5): Gram-Schmidt needs the second projection pass
+    (CGS2) for that, and FP32-level projections (SPLIT3); with the reference's FP16 products the
+    iterate stalls at FP16-level orthogonality."""
+    A = np.asarray(A, dtype=F32)
+    m, n = A.shape
+    alpha = np.linalg.norm(A.astype(np.float64))
+    X = (A / F32(alpha)).astype(F32)
+    if l0 is None:
+        _, R0 = rgsqrf(X, prec=prec)
+        l0 = 1.0 / np.linalg.norm(np.linalg.inv(np.triu(R0).astype(np.float64)))
+    l = float(l0)
+    tol1 = 10.0 * tol / 2.0
+    tol3 = tol1 ** (1.0 / 3.0)
+    it = 0
+    for it in range(1, max_iter + 1):
+        a, b, c, l = qdwh_coeffs(min(l, 1.0))
+        S = np.vstack([F32(np.sqrt(c)) * X, np.eye(n, dtype=F32)]).astype(F32)
+        Q, _ = rgsqrf(S, prec=prec, cgs2=True)
+        gp = "split3" if prec in ("split2", "split3") else prec
+        Xn = (F32(b / c) * X + F32((a - b / c) / np.sqrt(c)) * tc_gemm(Q[:m], Q[m:].T, gp)).astype(F32)
+        if symmetrize:
+            Xn = ((Xn + Xn.T) / 2).astype(F32)
+        diff = np.linalg.norm((Xn - X).astype(np.float64))
+        X = Xn
+        if diff < tol3 and 1.0 - l < tol1:
+            break
+    H = (X.astype(np.float64).T @ A.astype(np.float64))
+    H = ((H + H.T) / 2).astype(F32)
+    return X, H, it
+
+
+# --------------------------------------------------------------- sy2sb
+def sy2sb(A: np.ndarray, nb: int = 128, prec: str = "fp32"):
+    """Symmetric to band reduction B = Q^T A Q (bandwidth nb) — ssytrd_sy2sb,
+    EVD/later_sy2sb_blocked.cu:23-186, on one matrix updated in place. Per block
+    column i: rhouqr of the panel A[i+nb:, i:i+nb] (FP32 at nb <= 128), the panel
+    becomes [R; 0] (and its mirror above the diagonal), then the two-sided ZY
+    update of A22 = A[i+nb:, i+nb:]: P = A22 W, T = W^T P, Z = P - T-weighted Y / 2,
+    A22 -= Y Z^T + Z Y^T. Returns (B, Y, W) with the reflectors of each block
+    column in place (Q = prod_i (I - W_i Y_i^T))."""
+    a = np.array(A, dtype=F32)
+    n = a.shape[0]
+    Y = np.zeros((n, n), dtype=F32)
+    Wf = np.zeros((n, n), dtype=F32)
+
+    def gemm(x, y):
+        return (x @ y).astype(F32) if prec == "fp32" else tc_gemm(x, y, prec)
+
+    for i in range(0, n - nb, nb):
+        r0 = i + nb
+        y, w, r = rhouqr(a[r0:, i:i + nb], prec="fp16")
+        Y[r0:, i:i + nb] = y
+        Wf[r0:, i:i + nb] = w
+        pan = np.zeros_like(y)
+        pan[:nb] = np.triu(r)
+        a[r0:, i:i + nb] = pan
+        a[i:i + nb, r0:] = pan.T
+        a22 = a[r0:, r0:]
+        P = gemm(a22, w)
+        T = gemm(w.T, P)
+        Z = (P - F32(0.5) * gemm(y, T)).astype(F32)
+        a22 -= gemm(y, Z.T)
+        a22 -= gemm(Z, y.T)
+    return a, Y, Wf

@@ -32,7 +32,7 @@ def test_later_h_exports_cpp_symbols():
     if nm is None:
         pytest.skip("nm not available")
     out = subprocess.run([nm, "-DC", str(lg.build.build())], capture_output=True, text=True).stdout
-    for sym in ["later_rgsqrf(cudaCtxt", "later_rhouqr(cudaCtxt", "later_ormqr(int", "later_ormqr2(int",
+    for sym in ["later_rgsqrf(cudaCtxt", "later_rhouqr(cudaCtxt", "later_ormqr(int", "later_ormqr2(int", "later_bhouqr(int", "later_qdwh_polar(cudaCtxt", "later_sy2sb_rec(cudaCtxt", "ssytrd_sy2sb(cudaCtxt",
                 "later_rtrsm(cublasContext*", "later_rsyrk(cublasContext*", "later_rtrmm(int", "later_rpotrf(char",
                 "later_get_last_status()"]:
         assert sym in out, sym

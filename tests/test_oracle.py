@@ -138,3 +138,20 @@ def test_rpotrf_oracle_known_answer():
     assert np.linalg.norm(L3 - T) / np.linalg.norm(T) < 1e-3  # the factor of T T^T is T
     L16 = lo.rpotrf(A, prec="fp16", leaf=128).astype(np.float64)
     assert metrics.chol_backward_error(A, L16) < 1e-3
+
+
+@pytest.mark.parametrize("m,n", [(1000, 256), (700, 384)])
+def test_oracle_bhouqr_is_lapack_householder_form(m, n):
+    """later_bhouqr's restatement (FP32, the reference's arithmetic) gives LAPACK dgeqrf's reflectors and R,
+    and Q = I - W Y^T (the reference's later_ormqr2) is orthonormal with A = Q R."""
+    import scipy.linalg.lapack as la
+    A = gen.normal(m, n, seed=3)
+    Y, W, R = lo.bhouqr(A)
+    Q = lo.ormqr(W, Y)
+    qr, tau, _, _ = la.dgeqrf(A.astype(np.float64))
+    Rl = np.triu(qr[:n])
+    V = np.tril(qr, -1) + np.eye(m, n)
+    assert np.linalg.norm(R - Rl) / np.linalg.norm(Rl) < 2e-6
+    assert np.linalg.norm(Y - V) / np.linalg.norm(V) < 2e-6
+    assert metrics.qr_backward_error(A, Q, R) < 2e-6
+    assert metrics.orthogonality(Q) < 1e-4
