@@ -93,6 +93,45 @@ later_status_t later_c_rgsqrf(later_stream_t stream, int m, int n, float* A, int
                               float* work, int64_t lwork, void* hwork, int64_t lhwork,
                               const later_options_t* opt);
 
+/*
+ * later_c_rgsqrf with the matrix in host memory (no counterpart in the
+ * reference, whose callers copy A to the device themselves). hA (m x n,
+ * ldha) is copied to the device buffer A (lda) in chunks of columns on a
+ * copy stream, each chunk converted to 16 bits there; the factorisation
+ * waits for a chunk only where it first reads it. Q's columns and R's
+ * columns (rows on and above the diagonal) are copied back to hQ and hR in
+ * chunks as soon as the leaf that finishes them has run, while the rest of
+ * the factorisation proceeds. hQ may be hA. R (device, n x n, ldr) as in
+ * later_c_rgsqrf; entries of hR below the diagonal are not written. Host
+ * buffers must be pinned (cudaHostAlloc / cudaHostRegister) for the copies
+ * to overlap. The work is complete when `stream` reaches the point after
+ * this call. The copy streams are created on the first call from a host
+ * thread on a device and kept until exit.
+ */
+later_status_t later_c_rgsqrf_host(later_stream_t stream, int m, int n, const float* hA, int ldha, float* hQ,
+                                   int ldhq, float* hR, int ldhr, float* A, int lda, float* R, int ldr, float* work,
+                                   int64_t lwork, void* hwork, int64_t lhwork, const later_options_t* opt);
+
+/* Device bytes later_c_oc_rgsqrf needs for in-core panels of `panel` columns. */
+later_status_t later_c_oc_rgsqrf_bufsize(int m, int panel, const later_options_t* opt, int64_t* dev_bytes);
+
+/*
+ * Out-of-core recursive Gram-Schmidt QR: A (m x n, ldha) stays in host memory
+ * and is overwritten by Q; R (n x n, ldhr) is written to host memory in full
+ * (zeros below the diagonal). Replaces LATER include/LATER.h:49-51
+ * later_oc_qr_rec / later_oc_qr_blk (QR/later_oc_qr.cu:29-121, with the
+ * tiled host-device GEMM of BLAS/later_gemm.cu:52-189), whose signatures pass
+ * the reference's Mem_pool class. The work runs through the caller's device
+ * region `dev` (dev_bytes, 256-byte aligned): panels of `panel` columns (a
+ * multiple of 32; 0 = the widest power-of-two multiple of 128 that fits) are
+ * factored in core by rgsqrf after the projections against all earlier
+ * panels' Q, which are streamed back in on a copy stream and double-buffered
+ * against the tensor-core products. Host buffers must be pinned for the
+ * copies to overlap. Precision and CGS2 as later_c_rgsqrf.
+ */
+later_status_t later_c_oc_rgsqrf(later_stream_t stream, int m, int n, float* hA, int ldha, float* hR, int ldhr,
+                                 int panel, void* dev, int64_t dev_bytes, const later_options_t* opt);
+
 /* Minimum `work` (floats) and `hwork` (16-bit elements) for later_c_rhouqr. */
 later_status_t later_c_rhouqr_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork,
                                       int64_t* lhwork);

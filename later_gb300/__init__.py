@@ -19,7 +19,8 @@ from . import build as _build
 
 __all__ = [
     "LaterError", "Options", "PREC", "lib", "colmajor", "empty_colmajor",
-    "later_rgsqrf", "rgsqrf_bufsize", "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "later_bhouqr",
+    "later_rgsqrf", "rgsqrf_bufsize", "later_rgsqrf_host", "later_oc_rgsqrf", "oc_rgsqrf_bytes",
+    "later_rhouqr", "rhouqr_bufsize", "later_ormqr", "later_bhouqr",
     "bhouqr_bufsize", "later_ormqr2", "later_qdwh_polar", "qdwh_bufsize", "later_sy2sb",
     "sy2sb_bufsize", "later_rsyrk", "later_rtrsm",
     "later_rtrmm", "later_rpotrf", "blas3_bufsize",
@@ -101,6 +102,10 @@ _SIGS = {
     "later_c_rhouqr_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "later_c_rhouqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_ormqr": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i64]),
+    "later_c_oc_rgsqrf_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64)]),
+    "later_c_oc_rgsqrf": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _i, _vp, _i64, ctypes.POINTER(Options)]),
+    "later_c_rgsqrf_host": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64,
+                                 ctypes.POINTER(Options)]),
     "later_c_sy2sb_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "later_c_sy2sb": (_i, [_vp, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i64, _vp, _i64, ctypes.POINTER(Options)]),
     "later_c_qdwh_bufsize": (_i, [_i, _i, ctypes.POINTER(Options), ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
@@ -241,6 +246,42 @@ def later_rgsqrf(A, R=None, work=None, hwork=None, *, precision="fp16", cgs2=Fal
     _check(lib().later_c_rgsqrf(_stream(stream), m, n, A.data_ptr(), lda, R.data_ptr(), ldr, work.data_ptr(),
                                 work.numel(), hwork.data_ptr(), hwork.numel(), ctypes.byref(o)), "later_rgsqrf")
     return R
+
+
+def later_rgsqrf_host(hA, hQ, hR, A, R, work=None, hwork=None, *, precision="fp16", cgs2=False, leaf=128,
+                      panel="fused", stream=None):
+    """rgsqrf with host buffers: hA (pinned, column-major m x n) in; Q into hQ (may be hA) and the upper
+    triangle of R into hR, copied in and out in column chunks overlapped with the factorisation. A and R
+    are the device buffers it runs in. Asynchronous on `stream` like the other calls."""
+    import torch
+    m, n = hA.shape
+    lw, lh = rgsqrf_bufsize(m, n, precision, cgs2, leaf)
+    if work is None:
+        work = torch.empty(lw, dtype=torch.float32, device=A.device)
+    if hwork is None:
+        hwork = torch.empty(lh, dtype=torch.float16, device=A.device)
+    o = Options.make(precision, cgs2, leaf, 0, panel)
+    _check(lib().later_c_rgsqrf_host(_stream(stream), m, n, hA.data_ptr(), _ld(hA, "hA"), hQ.data_ptr(),
+                                     _ld(hQ, "hQ"), hR.data_ptr(), _ld(hR, "hR"), A.data_ptr(), _ld(A, "A"),
+                                     R.data_ptr(), _ld(R, "R"), work.data_ptr(), work.numel(), hwork.data_ptr(),
+                                     hwork.numel(), ctypes.byref(o)), "later_rgsqrf_host")
+
+
+def oc_rgsqrf_bytes(m, panel, precision="split2", cgs2=False):
+    o = Options.make(precision, cgs2)
+    b = ctypes.c_int64()
+    _check(lib().later_c_oc_rgsqrf_bufsize(m, panel, ctypes.byref(o), ctypes.byref(b)), "oc_rgsqrf_bufsize")
+    return b.value
+
+
+def later_oc_rgsqrf(hA, hR, dev, panel=0, *, precision="split2", cgs2=False, stream=None):
+    """Out-of-core QR: hA (host, column-major) becomes Q, hR receives R; `dev` is a device byte buffer
+    (torch uint8 tensor) the factorisation runs through (include/LATER.h:49-51 later_oc_qr_rec / _blk)."""
+    m, n = hA.shape
+    o = Options.make(precision, cgs2)
+    _check(lib().later_c_oc_rgsqrf(_stream(stream), m, n, hA.data_ptr(), _ld(hA, "hA"), hR.data_ptr(),
+                                   _ld(hR, "hR"), int(panel), dev.data_ptr(), dev.numel() * dev.element_size(),
+                                   ctypes.byref(o)), "later_oc_rgsqrf")
 
 
 def rhouqr_bufsize(m, n, precision="fp16"):

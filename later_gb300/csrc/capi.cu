@@ -68,6 +68,25 @@ later_status_t later_c_rgsqrf(later_stream_t stream, int m, int n, float* A, int
                 options_from(opt));
 }
 
+later_status_t later_c_rgsqrf_host(later_stream_t stream, int m, int n, const float* hA, int ldha, float* hQ,
+                                   int ldhq, float* hR, int ldhr, float* A, int lda, float* R, int ldr, float* work,
+                                   int64_t lwork, void* hwork, int64_t lhwork, const later_options_t* opt) {
+  return rgsqrf_host(reinterpret_cast<cudaStream_t>(stream), m, n, hA, ldha, hQ, ldhq, hR, ldhr, A, lda, R, ldr, work,
+                     lwork, hwork, lhwork, options_from(opt));
+}
+
+later_status_t later_c_oc_rgsqrf_bufsize(int m, int panel, const later_options_t* opt, int64_t* dev_bytes) {
+  if (m < 1 || panel < 32 || panel % 32 != 0) return LATER_ERR_INVALID_ARG;
+  if (dev_bytes) *dev_bytes = oc_rgsqrf_bytes(m, panel, options_from(opt));
+  return LATER_OK;
+}
+
+later_status_t later_c_oc_rgsqrf(later_stream_t stream, int m, int n, float* hA, int ldha, float* hR, int ldhr,
+                                 int panel, void* dev, int64_t dev_bytes, const later_options_t* opt) {
+  return oc_rgsqrf(reinterpret_cast<cudaStream_t>(stream), m, n, hA, ldha, hR, ldhr, panel, dev, dev_bytes,
+                   options_from(opt));
+}
+
 later_status_t later_c_rhouqr_bufsize(int m, int n, const later_options_t* opt, int64_t* lwork, int64_t* lhwork) {
   if (m < 1 || n < 1 || m < n) return LATER_ERR_INVALID_ARG;
   const QrNeed q = rhouqr_need(m, n, options_from(opt));

@@ -40,7 +40,8 @@ Options options_from(const later_options_t* o) {
 
 namespace {
 
-constexpr int kCounters = 4096 + 64;  // ints: [0,2048) panels, [2048,4096) GEMM split-K, then the fused leaf's sync
+constexpr int kCounters = 4096 + 64;
+constexpr int kMaxHostChunks = 64;  // ints: [0,2048) panels, [2048,4096) GEMM split-K, then the fused leaf's sync
 
 struct Ctx {
   cudaStream_t st;
@@ -56,6 +57,7 @@ struct Ctx {
   float* s_tmp;     // CGS2 second-pass coefficients (top-level size)
   int64_t lds;
   int m;
+  struct HostPipe* pipe = nullptr;  // host-buffer call: column chunks copied in and out around the recursion
 };
 
 inline char* col16(char* base, int64_t ld, int64_t j) { return base ? base + j * ld * 2 : nullptr; }
@@ -81,6 +83,69 @@ Scratch gemm_scratch(Ctx& c) {
   return s;
 }
 
+// Host-buffer rgsqrf (later_c_rgsqrf_host): A arrives from host memory and Q,
+// R go back, in chunks of columns, on two copy streams that run beside the
+// recursion. Chunk k is copied in and converted to 16 bits on the `in` stream;
+// the compute stream waits for it just before the first operation that reads
+// those columns (the chunk's first leaf, or the trailing update of the node
+// whose right half holds it). Once the leaf that finishes the chunk's last
+// column has run, its columns of Q and R are final: the `out` stream copies
+// them back while the recursion goes on.
+struct HostPipe {
+  cudaStream_t in = nullptr, out = nullptr;
+  int chunk = 0, nchunks = 0;
+  cudaEvent_t ready[kMaxHostChunks];  // chunk k on the device (and converted), recorded on `in`
+  cudaEvent_t done[kMaxHostChunks];   // chunk k final, recorded on the compute stream
+  int waited = 0;                     // chunks [0, waited) already waited for on the compute stream
+  int sent = 0;                       // chunks [0, sent) queued for copy-out
+  const float* hA = nullptr;
+  int64_t ldha = 0;
+  float* hQ = nullptr;
+  int64_t ldhq = 0;
+  float* hR = nullptr;
+  int64_t ldhr = 0;
+  float* A = nullptr;
+  int64_t lda = 0;
+  float* R = nullptr;
+  int64_t ldr = 0;
+  int n = 0;
+};
+
+// The compute stream waits until columns [0, col_end) are on the device.
+later_status_t pipe_need(Ctx& c, int64_t col_end) {
+  HostPipe* p = c.pipe;
+  if (!p) return LATER_OK;
+  const int k_end = static_cast<int>(std::min<int64_t>(p->nchunks, (col_end + p->chunk - 1) / p->chunk));
+  if (k_end > p->waited) {
+    LATER_CHECK_CUDA(cudaStreamWaitEvent(c.st, p->ready[k_end - 1], 0));  // `in` is in order
+    p->waited = k_end;
+  }
+  return LATER_OK;
+}
+
+// Columns [0, col_end) of Q and R are final: queue the completed chunks' copy-out.
+later_status_t pipe_done(Ctx& c, int64_t col_end) {
+  HostPipe* p = c.pipe;
+  if (!p) return LATER_OK;
+  const int k_end = static_cast<int>(std::min<int64_t>(p->nchunks, col_end / p->chunk +
+                                                                       (col_end >= p->n ? 1 : 0)));
+  for (int k = p->sent; k < k_end; ++k) {
+    const int64_t c0 = static_cast<int64_t>(k) * p->chunk;
+    const int64_t w = std::min<int64_t>(p->chunk, p->n - c0);
+    LATER_CHECK_CUDA(cudaEventRecord(p->done[k], c.st));
+    LATER_CHECK_CUDA(cudaStreamWaitEvent(p->out, p->done[k], 0));
+    LATER_CHECK_CUDA(cudaMemcpy2DAsync(p->hQ + c0 * p->ldhq, p->ldhq * sizeof(float), p->A + c0 * p->lda,
+                                       p->lda * sizeof(float), c.m * sizeof(float), w, cudaMemcpyDeviceToHost,
+                                       p->out));
+    // R's column block, rows [0, c0 + w): the part on and above the diagonal
+    LATER_CHECK_CUDA(cudaMemcpy2DAsync(p->hR + c0 * p->ldhr, p->ldhr * sizeof(float), p->R + c0 * p->ldr,
+                                       p->ldr * sizeof(float), (c0 + w) * sizeof(float), w, cudaMemcpyDeviceToHost,
+                                       p->out));
+  }
+  if (k_end > p->sent) p->sent = k_end;
+  return LATER_OK;
+}
+
 later_status_t leaf_qr(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
   if (w <= 32) {
     return tsqr_panel(c.st, c.m, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
@@ -103,14 +168,19 @@ later_status_t leaf_qr(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t l
 // A leaf: one fused launch (leaf.cu) unless the caller asked for the
 // reference's panel algorithm or the device / workspace cannot run it.
 later_status_t leaf_top(Ctx& c, int w, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
+  LATER_CHECK(pipe_need(c, col + w));
   if ((c.o.panel == 0 || c.o.panel == 2) && w <= kLeafMaxWidth) {
     const later_status_t s =
         leaf_fused(c.st, c.m, w, A, lda, R, ldr, col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh,
                    panel_out_prec(c.o.prec), c.o.cgs2, c.o.panel == 2, *c.ws, c.counters + 4096, c.counters,
                    c.o.budget, nullptr);
-    if (s != LATER_ERR_NOT_SUPPORTED && s != LATER_ERR_WORKSPACE) return s;
+    if (s != LATER_ERR_NOT_SUPPORTED && s != LATER_ERR_WORKSPACE) {
+      LATER_CHECK(s);
+      return pipe_done(c, col + w);
+    }
   }
-  return leaf_qr(c, w, A, lda, R, ldr, col);
+  LATER_CHECK(leaf_qr(c, w, A, lda, R, ldr, col));
+  return pipe_done(c, col + w);
 }
 
 later_status_t rec_qr(Ctx& c, int n, float* A, int64_t lda, float* R, int64_t ldr, int64_t col) {
@@ -122,6 +192,7 @@ later_status_t rec_qr(Ctx& c, int n, float* A, int64_t lda, float* R, int64_t ld
   Op16 Q1{col16(c.sh_hi, c.ldh, col), col16(c.sh_lo, c.ldh, col), c.ldh};
   Op16 A2h{col16(c.sh_hi, c.ldh, col + n1), col16(c.sh_lo, c.ldh, col + n1), c.ldh};
   Op16 R12h{c.r12h, c.r12l, c.ldr12};
+  LATER_CHECK(pipe_need(c, col + n));  // the update reads all of A2
   const int passes = c.o.cgs2 ? 2 : 1;
   for (int pass = 0; pass < passes; ++pass) {
     // R12 (+)= Q1^T A2, FP32 into R, 16-bit copy of this pass's product. In
@@ -229,8 +300,92 @@ QrNeed rgsqrf_need(int m, int n, const Options& o) {
   return q;
 }
 
+namespace {
+
+// Copy streams and events of the host-buffer variant, one set per host thread
+// and device, created on first use and kept until exit.
+struct PipeRes {
+  bool ready = false;
+  cudaStream_t in = nullptr, out = nullptr;
+  cudaEvent_t ready_ev[kMaxHostChunks], done_ev[kMaxHostChunks], start = nullptr, end = nullptr;
+};
+
+later_status_t pipe_resources(PipeRes** out) {
+  static thread_local PipeRes res[16];
+  int dev = 0;
+  LATER_CHECK_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 16) return LATER_ERR_NOT_SUPPORTED;
+  PipeRes& r = res[dev];
+  if (!r.ready) {
+    LATER_CHECK_CUDA(cudaStreamCreateWithFlags(&r.in, cudaStreamNonBlocking));
+    LATER_CHECK_CUDA(cudaStreamCreateWithFlags(&r.out, cudaStreamNonBlocking));
+    for (int k = 0; k < kMaxHostChunks; ++k) {
+      LATER_CHECK_CUDA(cudaEventCreateWithFlags(&r.ready_ev[k], cudaEventDisableTiming));
+      LATER_CHECK_CUDA(cudaEventCreateWithFlags(&r.done_ev[k], cudaEventDisableTiming));
+    }
+    LATER_CHECK_CUDA(cudaEventCreateWithFlags(&r.start, cudaEventDisableTiming));
+    LATER_CHECK_CUDA(cudaEventCreateWithFlags(&r.end, cudaEventDisableTiming));
+    r.ready = true;
+  }
+  *out = &r;
+  return LATER_OK;
+}
+
+later_status_t rgsqrf_impl(cudaStream_t st, int m, int n, float* A, int64_t lda, float* R, int64_t ldr, float* work,
+                           int64_t lwork, void* hwork, int64_t lhwork, const Options& o, HostPipe* pipe);
+
+}  // namespace
+
 later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, float* R, int64_t ldr, float* work,
                       int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
+  return rgsqrf_impl(st, m, n, A, lda, R, ldr, work, lwork, hwork, lhwork, o, nullptr);
+}
+
+later_status_t rgsqrf_host(cudaStream_t st, int m, int n, const float* hA, int64_t ldha, float* hQ, int64_t ldhq,
+                           float* hR, int64_t ldhr, float* A, int64_t lda, float* R, int64_t ldr, float* work,
+                           int64_t lwork, void* hwork, int64_t lhwork, const Options& o) {
+  if (!hA || !hQ || !hR || ldha < m || ldhq < m || ldhr < n) return LATER_ERR_INVALID_ARG;
+  PipeRes* res = nullptr;
+  LATER_CHECK(pipe_resources(&res));
+  HostPipe p;
+  p.in = res->in;
+  p.out = res->out;
+  const int units = (n + o.leaf - 1) / std::max(o.leaf, 1);
+  const int per = (units + kMaxHostChunks - 1) / kMaxHostChunks;  // leaves per chunk
+  p.chunk = std::max(1, per) * o.leaf;
+  p.nchunks = (n + p.chunk - 1) / p.chunk;
+  for (int k = 0; k < p.nchunks; ++k) {
+    p.ready[k] = res->ready_ev[k];
+    p.done[k] = res->done_ev[k];
+  }
+  p.hA = hA;
+  p.ldha = ldha;
+  p.hQ = hQ;
+  p.ldhq = ldhq;
+  p.hR = hR;
+  p.ldhr = ldhr;
+  p.A = A;
+  p.lda = lda;
+  p.R = R;
+  p.ldr = ldr;
+  p.n = n;
+  // the copy streams start after the caller's earlier work on `st`
+  LATER_CHECK_CUDA(cudaEventRecord(res->start, st));
+  LATER_CHECK_CUDA(cudaStreamWaitEvent(p.in, res->start, 0));
+  LATER_CHECK_CUDA(cudaStreamWaitEvent(p.out, res->start, 0));
+  const later_status_t s = rgsqrf_impl(st, m, n, A, lda, R, ldr, work, lwork, hwork, lhwork, o, &p);
+  // `st` completes only after the last copy-out (also on failure: nothing may still write the caller's buffers)
+  LATER_CHECK_CUDA(cudaEventRecord(res->end, p.out));
+  LATER_CHECK_CUDA(cudaStreamWaitEvent(st, res->end, 0));
+  LATER_CHECK_CUDA(cudaEventRecord(res->end, p.in));
+  LATER_CHECK_CUDA(cudaStreamWaitEvent(st, res->end, 0));
+  return s;
+}
+
+namespace {
+
+later_status_t rgsqrf_impl(cudaStream_t st, int m, int n, float* A, int64_t lda, float* R, int64_t ldr, float* work,
+                           int64_t lwork, void* hwork, int64_t lhwork, const Options& o, HostPipe* pipe) {
   if (m < 1 || n < 1 || m < n || lda < m || ldr < n || !A || !R) return LATER_ERR_INVALID_ARG;
   if (o.leaf != 32 && o.leaf != 64 && o.leaf != 128) return LATER_ERR_INVALID_ARG;
   if (o.prec < LATER_PREC_FP16 || o.prec > LATER_PREC_SPLIT2) return LATER_ERR_INVALID_ARG;
@@ -260,11 +415,31 @@ later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, floa
   LATER_CHECK(fill_strict_lower(st, n, n, R, ldr, 0.f));
   const int f = first_leaf(n, o.leaf);
   // The columns' 16-bit copy as the projections read it (SPLIT2: hi only).
-  LATER_CHECK(convert16(st, m, n - f, A + static_cast<int64_t>(f) * lda, lda, c.sh_hi + f * c.ldh * 2,
-                        (c.sh_lo && o.prec == LATER_PREC_SPLIT3) ? c.sh_lo + f * c.ldh * 2 : nullptr, c.ldh,
-                        proj_prec(o.prec)));
+  auto convert_cols = [&](cudaStream_t s, int64_t c0, int64_t c1) -> later_status_t {
+    c0 = std::max<int64_t>(c0, f);
+    if (c1 <= c0) return LATER_OK;
+    return convert16(s, m, static_cast<int>(c1 - c0), A + c0 * lda, lda, c.sh_hi + c0 * c.ldh * 2,
+                     (c.sh_lo && o.prec == LATER_PREC_SPLIT3) ? c.sh_lo + c0 * c.ldh * 2 : nullptr, c.ldh,
+                     proj_prec(o.prec));
+  };
+  if (pipe) {
+    c.pipe = pipe;
+    for (int k = 0; k < pipe->nchunks; ++k) {
+      const int64_t c0 = static_cast<int64_t>(k) * pipe->chunk;
+      const int64_t w = std::min<int64_t>(pipe->chunk, n - c0);
+      LATER_CHECK_CUDA(cudaMemcpy2DAsync(A + c0 * lda, lda * sizeof(float), pipe->hA + c0 * pipe->ldha,
+                                         pipe->ldha * sizeof(float), m * sizeof(float), w, cudaMemcpyHostToDevice,
+                                         pipe->in));
+      LATER_CHECK(convert_cols(pipe->in, c0, c0 + w));
+      LATER_CHECK_CUDA(cudaEventRecord(pipe->ready[k], pipe->in));
+    }
+  } else {
+    LATER_CHECK(convert_cols(st, 0, n));
+  }
   return rec_qr(c, n, A, lda, R, ldr, 0);
 }
+
+}  // namespace
 
 // ======================================================================
 // Recursive Householder QR (QR/later_rhouqr.cu:27-201):

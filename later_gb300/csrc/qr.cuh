@@ -28,6 +28,18 @@ QrNeed rgsqrf_need(int m, int n, const Options& o);
 later_status_t rgsqrf(cudaStream_t st, int m, int n, float* A, int64_t lda, float* R, int64_t ldr, float* work,
                       int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
 
+// rgsqrf on host buffers: hA is copied in and Q, R copied out in column
+// chunks on two copy streams overlapped with the factorisation (A, R are the
+// device buffers it runs in); `st` completes after the last copy.
+later_status_t rgsqrf_host(cudaStream_t st, int m, int n, const float* hA, int64_t ldha, float* hQ, int64_t ldhq,
+                           float* hR, int64_t ldhr, float* A, int64_t lda, float* R, int64_t ldr, float* work,
+                           int64_t lwork, void* hwork, int64_t lhwork, const Options& o);
+
+// Out-of-core rgsqrf through a caller-given device region (oc.cu).
+int64_t oc_rgsqrf_bytes(int m, int panel, const Options& o);
+later_status_t oc_rgsqrf(cudaStream_t st, int m, int n, float* hA, int64_t ldha, float* hR, int64_t ldhr, int panel,
+                         void* dev, int64_t dev_bytes, const Options& o);
+
 QrNeed rhouqr_need(int m, int n, const Options& o);
 
 later_status_t rhouqr(cudaStream_t st, int m, int n, float* A, int64_t lda, float* W, int64_t ldw, float* R,

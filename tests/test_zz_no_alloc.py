@@ -55,6 +55,11 @@ def test_noalloc_matches_gemm16_twice(cuda, ta, tb, m, n, k):
         assert lg.device_status() == 0
         err = float((D.double() - ref.double()).norm() / ref.double().norm())
         assert err < _rel_tol(k), err
+        # and against the exact product of the same 16-bit operands, in FP64
+        a = A.double() if ta == "N" else A.double().t()
+        exact = a @ B.double()
+        err64 = float((D.double() - exact).norm() / exact.norm())
+        assert err64 < _rel_tol(k), err64
 
 
 def test_noalloc_rejects_outputs_beyond_the_array(cuda):
