@@ -1,5 +1,5 @@
 // A client written against LATER.h the way the reference's tests call it
-// (test/test_qr.cu:66-136, test/test_potrf.cu, test/test_trsm.cu): buffers
+// (test/test_qr.cu:66-176, test/test_potrf.cu, test/test_trsm.cu): buffers
 // sized as the reference sizes them, a cudaCtxt, and no other API. Checks
 // each result on the host in double precision; exit code 0 = all within bounds.
 #include <cmath>
@@ -82,6 +82,17 @@ int main() {
   double e2 = qr_bwd(m, n, hA, Q, hR);
   std::printf("later_rhouqr+ormqr status %d  ||A-QR||/||A|| = %.3e\n", (int)later_get_last_status(), e2);
   fails += (later_get_last_status() != LATER_OK || !(e2 < 5e-4));
+
+  // bhouqr + ormqr2 with the reference test's buffers (test/test_qr.cu:140-176, algo 3)
+  CK(cudaMemcpy(A, hA.data(), sizeof(float) * m * n, cudaMemcpyHostToDevice));
+  later_bhouqr(m, n, A, m, W, m, R, n, work, m * n, hwork, m * n, U);
+  later_ormqr2(m, n, W, m, A, m, work);
+  CK(cudaDeviceSynchronize());
+  CK(cudaMemcpy(Q.data(), W, sizeof(float) * m * n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hR.data(), R, sizeof(float) * n * n, cudaMemcpyDeviceToHost));
+  double e2b = qr_bwd(m, n, hA, Q, hR);
+  std::printf("later_bhouqr+ormqr2 status %d  ||A-QR||/||A|| = %.3e\n", (int)later_get_last_status(), e2b);
+  fails += (later_get_last_status() != LATER_OK || !(e2b < 3e-6));
 
   // rpotrf on the reference test's SPD input T T^T, T = tril(0.1) (test/test_potrf.cu:38-62)
   const int np = 512;

@@ -38,7 +38,8 @@ def test_sy2sb_band_eigenvalues_and_similarity(cuda, n, nb, prec, tol):
     assert lg.device_status() == 0
     B = dA.cpu().numpy()
     assert np.all(np.triu(B, nb + 1) == 0) and np.all(np.tril(B, -nb - 1) == 0)
-    assert np.array_equal(B, B.T)
+    # symmetric to rounding: entry (i, j) and (j, i) take the two rank-nb products in opposite order
+    assert np.abs(B - B.T).max() <= 10 * tol * np.abs(A).max()
     ev = np.linalg.eigvalsh(B.astype(np.float64))
     ev0 = np.linalg.eigvalsh(A.astype(np.float64))
     assert np.abs(ev - ev0).max() <= tol * np.abs(ev0).max(), np.abs(ev - ev0).max()
