@@ -699,6 +699,33 @@ def spd_result(a, n, kappa, precision, steps, warmup, cpu=True, ref=None):
         if it >= warmup:
             ts.append(e0.elapsed_time(e1))
     fact_ms = statistics.median(ts)
+    # the same factorisation captured once in a CUDA graph and replayed (its ~1800 launches are small: the
+    # graph shows how much of the direct call's time is launch overhead)
+    graph_ms = None
+    try:
+        cs = torch.cuda.Stream()
+        cs.wait_stream(torch.cuda.current_stream())
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(cs):
+            F.copy_(A)
+            lg.later_rpotrf("l", n, F, precision=precision, work=work, hwork=hwork, stream=cs)
+            torch.cuda.synchronize()
+            with torch.cuda.graph(graph, stream=cs):
+                lg.later_rpotrf("l", n, F, precision=precision, work=work, hwork=hwork, stream=cs)
+        gts = []
+        for _ in range(max(steps, 2)):
+            F.copy_(A)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            graph.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            gts.append(e0.elapsed_time(e1))
+        graph_ms = statistics.median(gts)
+        del graph
+    except Exception as e:  # noqa: BLE001
+        graph_ms = f"not captured: {type(e).__name__}: {e}"
     del work, hwork
     t0 = time.perf_counter()
     X, info = lg.spd_solve(A, B, precision=precision, max_iter=60, tol=1e-12)
@@ -711,6 +738,8 @@ def spd_result(a, n, kappa, precision, steps, warmup, cpu=True, ref=None):
                        f"{k} RHS to backward error 1e-12",
            "value": ach, "unit": "TFLOP/s (n^3/3)", "ms_per_step": fact_ms, "steps": steps,
            "factor_status": st, "solve": {"seconds_incl_factor": solve_s, **info},
+           "graph_replay": ({"ms_per_step": graph_ms, "value": flops / graph_ms / 1e9}
+                            if isinstance(graph_ms, float) else graph_ms),
            "roofline": {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
                         "peak_source": "measured bf16 burst (MEASURED_PEAKS.json)"},
            "input_build_s": t_gen}

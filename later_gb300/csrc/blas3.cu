@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "blas3.cuh"
 #include "dense_dev.cuh"
@@ -351,6 +352,99 @@ __global__ void __launch_bounds__(256) trmm_leaf(int nb, int n, const float* __r
   }
 }
 
+// Inverse of the nb x nb lower-triangular L in shared memory (nb <= 128;
+// L[i][j] at Lc[j * ldc + i], ldc a multiple of 4) into V (same layout, zeros
+// above the diagonal). 32 x 32 blocks: warp c inverts diagonal block c by
+// forward substitution, lane = column of the inverse; then, by growing
+// distance d = I - J from the diagonal, T_J = sum_{K=J}^{I-1} L_IK V_KJ and
+// V_IJ = -V_II T_J, the blocks of one distance in parallel, 64 threads per
+// block in 4 x 4 register tiles (T: 3 x 32 x 36 floats of scratch). Rows and
+// columns of V beyond nb are zero. All threads call it.
+__device__ void tri_inverse_smem(int nb, const float* Lc, int ldc, float* V, float* T) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nblk = (nb + 31) / 32, np = nblk * 32;
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) V[(e / np) * ldc + e % np] = 0.f;
+  __syncthreads();
+  if (warp < nblk) {
+    const int cb = warp * 32, w = min(32, nb - cb);
+    float y[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) y[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      if (k < w) {
+        const float* dcol = Lc + (cb + k) * ldc + cb;  // column k of the diagonal block
+        y[k] = y[k] / dcol[k];
+#pragma unroll
+        for (int i = k + 1; i < 32; ++i)
+          if (i < w) y[i] -= dcol[i] * y[k];
+      }
+    }
+    if (lane < w) {
+#pragma unroll
+      for (int i = 0; i < 32; ++i)
+        if (i < w) V[(cb + lane) * ldc + cb + i] = y[i];
+    }
+  }
+  __syncthreads();
+  const int blk = threadIdx.x / 64, t = threadIdx.x % 64;
+  const int r0 = 4 * (t % 8), c0 = 4 * (t / 8);  // this thread's 4 x 4 tile inside a 32 x 32 block
+  for (int d = 1; d < nblk; ++d) {
+    const bool act = blk < nblk - d;
+    const int J = blk, I = blk + d;
+    if (act) {
+      float acc[4][4] = {};
+      const int rowI = I * 32 + r0;
+#pragma unroll 4
+      for (int k = J * 32; k < I * 32; ++k) {
+        // rows of L at or beyond nb hold whatever the caller's staging left there: masked, so that
+        // T's rows there are zero (they meet zero columns of V_II below)
+        const float4 a = *reinterpret_cast<const float4*>(&Lc[k * ldc + rowI]);
+        const float av[4] = {rowI < nb ? a.x : 0.f, rowI + 1 < nb ? a.y : 0.f, rowI + 2 < nb ? a.z : 0.f,
+                             rowI + 3 < nb ? a.w : 0.f};
+        float bv[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) bv[v] = V[(J * 32 + c0 + v) * ldc + k];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        *reinterpret_cast<float4*>(&T[J * 1152 + (r0 + u) * 36 + c0]) =
+            make_float4(acc[u][0], acc[u][1], acc[u][2], acc[u][3]);
+    }
+    __syncthreads();
+    if (act) {
+      float acc[4][4] = {};
+      const int rowI = I * 32 + r0;
+#pragma unroll 4
+      for (int k = 0; k < 32; ++k) {
+        const float4 a = *reinterpret_cast<const float4*>(&V[(I * 32 + k) * ldc + rowI]);
+        const float4 b = *reinterpret_cast<const float4*>(&T[J * 1152 + k * 36 + c0]);
+        const float av[4] = {a.x, a.y, a.z, a.w};
+        const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+        *reinterpret_cast<float4*>(&V[(J * 32 + c0 + v) * ldc + rowI]) =
+            make_float4(-acc[0][v], -acc[1][v], -acc[2][v], -acc[3][v]);
+    }
+    __syncthreads();
+  }
+  // entries of the padding (rows or columns >= nb) must stay zero for the caller
+  for (int e = threadIdx.x; e < np * np; e += blockDim.x) {
+    const int i = e % np, j = e / np;
+    if (i >= nb || j >= nb) V[j * ldc + i] = 0.f;
+  }
+  __syncthreads();
+}
+
 // Lower Cholesky of an nb x nb block (nb <= 128) in one CTA, in shared memory
 // (column-major, stride LDL), right-looking over 32-column blocks. Warp 0
 // factors the 32 x 32 diagonal block with the compact register-window
@@ -432,6 +526,41 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
   }
 }
 
+// Inverses of diagonal blocks of a lower-triangular factor, one CTA per block
+// (block i: columns [col[i], col[i] + w[i]) of L, w[i] <= 128), written as hi +
+// lo 16-bit pairs (ld 128) to slot col[i] / 64 of the tables.
+constexpr int kMaxInvBlocks = 160;
+struct InvBlocks {
+  int n;
+  int col[kMaxInvBlocks];
+  int w[kMaxInvBlocks];
+};
+
+__global__ void __launch_bounds__(256) trtri_blocks_kernel(const float* __restrict__ L, int64_t ldl, InvBlocks blocks,
+                                                           __half* vh_tab, __half* vl_tab) {
+  extern __shared__ __align__(16) float sm[];
+  float* Lc = sm;
+  float* V = sm + LDL * NB;
+  float* T = V + LDL * NB;
+  const int c = blocks.col[blockIdx.x], nb = blocks.w[blockIdx.x];
+  stage_cols(nb, L + c + static_cast<int64_t>(c) * ldl, ldl, Lc, LDL);
+  __syncthreads();
+  tri_inverse_smem(nb, Lc, LDL, V, T);
+  __half* vh = vh_tab + static_cast<int64_t>(c / 64) * (128 * 128);
+  __half* vl = vl_tab + static_cast<int64_t>(c / 64) * (128 * 128);
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int i = e % nb, j = e / nb;
+    const float v = V[j * LDL + i];
+    const __half h = __float2half_rn(v);
+    vh[i + j * 128] = h;
+    vl[i + j * 128] = __float2half_rn((v - __half2float(h)) * 2048.f);
+  }
+}
+
+constexpr size_t kPotrfLeafSmem = (LDL * NB) * sizeof(float) + (sizeof(PotrfSmem) + 15) / 16 * 16;
+constexpr size_t kTrtriSmem = (2 * LDL * NB + 3 * 1152) * sizeof(float);
+static_assert(kTrtriSmem <= 227 * 1024, "block inverse shared memory");
+
 inline int mode_of(int prec) { return prec == LATER_PREC_BF16 ? 1 : (prec == LATER_PREC_SPLIT3 ? 2 : 0); }
 
 // Splits n in half, rounded to a multiple of 64 (keeps 16-bit row offsets
@@ -464,7 +593,22 @@ struct B3 {
   char* h;      // 16-bit scratch (hwork) cursor
   size_t hcap;  // bytes
   Scratch sc;   // split-K scratch
+  // Cholesky only: the updates below the FP32 thresholds run as SPLIT3 tensor-core products (FP32-level)
+  // instead of SIMT FP32 ones, and, when inv_hi is set, the triangular solves against a diagonal block of
+  // the factor are products with that block's inverse, kept by the Cholesky leaves at slot col / 64.
+  bool tc_small = false;
+  bool leaf_gemm = false;
+  __half* inv_hi = nullptr;
+  __half* inv_lo = nullptr;
+  std::vector<char>* inv_done = nullptr;  // per slot: inverse already in the table
 };
+
+// Solves with at least this many rows use the diagonal block's inverse (its
+// one-off inversion is then cheaper than the substitution it replaces).
+constexpr int kInvMinRows = 2048;
+
+constexpr int64_t kInvSlot = 128 * 128;  // 16-bit elements per inverse block (ld 128)
+inline int64_t inv_slots(int n) { return (n + 63) / 64; }
 
 // Takes `elems` 16-bit elements from the hwork scratch (256-byte aligned).
 char* take16(B3& b, int64_t elems, size_t* mark) {
@@ -519,7 +663,35 @@ later_status_t gemm(B3& b, char ta, char tb, int M, int N, int K, float alpha, c
 // X L^T = B, L n x n, B m x n. X's 16-bit copy goes to (xh, ldh) (columns as B).
 // Updates are FP32 while n <= fp32_lim, tensor-core above.
 later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float* B, int64_t ldb, char* xh, char* xl,
-                        int64_t ldh, int fp32_lim = kFp32Trsm) {
+                        int64_t ldh, int fp32_lim = kFp32Trsm, int64_t col = -1) {
+  if (n <= NB && b.leaf_gemm && b.inv_hi && col >= 0 && m >= kInvMinRows && b.inv_done &&
+      (*b.inv_done)[col / 64]) {
+    // X = B L^-T as one SPLIT3 tensor-core product with the block's inverse (FP32-level operands)
+    B3 sub = b;
+    sub.o.prec = LATER_PREC_SPLIT3;
+    Op16 bb;
+    size_t used = 0;
+    LATER_CHECK(copy16(sub, m, n, B, ldb, &bb, &used));
+    sub.h += used;
+    sub.hcap -= used;
+    const Op16 vinv{b.inv_hi + (col / 64) * kInvSlot, b.inv_lo + (col / 64) * kInvSlot, 128};
+    GemmCall g;
+    g.ta = 'N';
+    g.tb = 'T';
+    g.M = m;
+    g.N = n;
+    g.K = n;
+    g.A = bb;
+    g.B = vinv;
+    g.out.D = B;
+    g.out.ldd = ldb;
+    g.out.Dh = xh;
+    g.out.Dl = xl;
+    g.out.ldh = ldh;
+    g.prec = LATER_PREC_SPLIT3;
+    g.out_prec = b.o.prec;
+    return tc_gemm(g, sub.sc, b.st, b.o.budget);
+  }
   if (n <= NB) {
     const size_t smem = (LDL * NB + 64 * XS) * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(trsm_rlt_leaf), smem)) return LATER_ERR_CUDA;
@@ -531,9 +703,22 @@ later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float*
     return cuda_status(cudaGetLastError());
   }
   const int n1 = half64(n), n2 = n - n1;
-  LATER_CHECK(trsm_rlt(b, m, n1, L, ldl, B, ldb, xh, xl, ldh, fp32_lim));
+  LATER_CHECK(trsm_rlt(b, m, n1, L, ldl, B, ldb, xh, xl, ldh, fp32_lim, col));
   // B2 -= X1 L21^T   (L21 = L[n1:, :n1], n2 x n1)
-  if (n <= fp32_lim) {
+  if (n <= fp32_lim && b.tc_small) {
+    // FP32-level: both operands freshly split into SPLIT3 pairs
+    B3 sub = b;
+    sub.o.prec = LATER_PREC_SPLIT3;
+    Op16 x1, l21;
+    size_t used = 0;
+    LATER_CHECK(copy16(sub, m, n1, B, ldb, &x1, &used));
+    sub.h += used;
+    sub.hcap -= used;
+    LATER_CHECK(copy16(sub, n2, n1, L + n1, ldl, &l21, &used));
+    sub.h += used;
+    sub.hcap -= used;
+    LATER_CHECK(gemm(sub, 'N', 'T', m, n2, n1, -1.f, x1, l21, 1.f, B + n1 * ldb, ldb));
+  } else if (n <= fp32_lim) {
     LATER_CHECK(simt_gemm_acc(b.st, m, n1, n2, -1.f, B, ldb, L + n1, ldl, 1, 0, B + n1 * ldb, ldb));
   } else {
     B3 sub = b;
@@ -546,7 +731,7 @@ later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float*
     LATER_CHECK(gemm(sub, 'N', 'T', m, n2, n1, -1.f, x1, l21, 1.f, B + n1 * ldb, ldb));
   }
   return trsm_rlt(b, m, n2, L + n1 + n1 * ldl, ldl, B + n1 * ldb, ldb, xh ? xh + n1 * ldh * 2 : nullptr,
-                  xl ? xl + n1 * ldh * 2 : nullptr, ldh, fp32_lim);
+                  xl ? xl + n1 * ldh * 2 : nullptr, ldh, fp32_lim, col >= 0 ? col + n1 : -1);
 }
 
 // L X = B, L m x m, B m x n. X's 16-bit copy goes to (xh, ldh) (rows as B).
@@ -639,9 +824,27 @@ later_status_t trmm_rec(B3& b, int m, int n, const float* L, int64_t ldl, const 
   return gemm(sub, 'N', 'N', m2, n, m1, 1.f, l21, bh, 1.f, C + m1, ldc);
 }
 
-later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda) {
+// The Cholesky leaves of an n-column block starting at column c (the same
+// half64 recursion as potrf_rec); those whose slot is not marked in `done`
+// are appended to `out` and marked.
+void leaf_blocks(int n, int c, InvBlocks* out, std::vector<char>& done) {
   if (n <= NB) {
-    const size_t smem = NB * LDL * sizeof(float) + sizeof(PotrfSmem);
+    if (!done[c / 64] && out->n < kMaxInvBlocks) {
+      out->col[out->n] = c;
+      out->w[out->n] = n;
+      ++out->n;
+      done[c / 64] = 1;
+    }
+    return;
+  }
+  const int n1 = half64(n);
+  leaf_blocks(n1, c, out, done);
+  leaf_blocks(n - n1, c + n1, out, done);
+}
+
+later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
+  if (n <= NB) {
+    const size_t smem = kPotrfLeafSmem;
     if (!smem_attr(reinterpret_cast<const void*>(potrf_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_PANEL);
     potrf_leaf<<<1, 256, smem, b.st>>>(n, A, lda, device_status_ptr());
@@ -649,7 +852,19 @@ later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda) {
     return cuda_status(cudaGetLastError());
   }
   const int n1 = half64(n), n2 = n - n1;
-  LATER_CHECK(potrf_rec(b, n1, A, lda));
+  LATER_CHECK(potrf_rec(b, n1, A, lda, col));
+  if (b.leaf_gemm && b.inv_hi && b.inv_done && n2 >= kInvMinRows) {
+    // the solve below has n2 rows: invert L11's diagonal blocks that are not inverted yet, all in one launch
+    InvBlocks blk{};
+    leaf_blocks(n1, static_cast<int>(col), &blk, *b.inv_done);
+    if (blk.n > 0) {
+      if (!smem_attr(reinterpret_cast<const void*>(trtri_blocks_kernel), kTrtriSmem)) return LATER_ERR_CUDA;
+      // A points at the diagonal block starting at column `col`; the kernel takes the factor's origin
+      trtri_blocks_kernel<<<blk.n, 256, kTrtriSmem, b.st>>>(A - col - col * lda, lda, blk, b.inv_hi, b.inv_lo);
+      note_launch();
+      LATER_CHECK_CUDA(cudaGetLastError());
+    }
+  }
   const bool fp32 = n <= kFp32Potrf;
   // A21 <- A21 L11^{-T}; its 16-bit copy is written by the solve.
   const int64_t ldx = round_up(n2, 8);
@@ -660,15 +875,24 @@ later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda) {
   B3 sub = b;
   sub.h += used;
   sub.hcap -= used;
-  LATER_CHECK(trsm_rlt(sub, n2, n1, A, lda, A + n1, lda, xh, xl, ldx, fp32 ? n1 : kFp32Trsm));
+  LATER_CHECK(trsm_rlt(sub, n2, n1, A, lda, A + n1, lda, xh, xl, ldx, fp32 ? n1 : kFp32Trsm, col));
   // A22 <- A22 - A21 A21^T (lower triangle only)
-  if (fp32) {
+  if (fp32 && b.tc_small) {
+    B3 s3 = sub;
+    s3.o.prec = LATER_PREC_SPLIT3;
+    Op16 x;
+    size_t u3 = 0;
+    LATER_CHECK(copy16(s3, n2, n1, A + n1, lda, &x, &u3));
+    s3.h += u3;
+    s3.hcap -= u3;
+    LATER_CHECK(gemm(s3, 'N', 'T', n2, n2, n1, -1.f, x, x, 1.f, A + n1 + n1 * lda, lda, nullptr, nullptr, 0, 1));
+  } else if (fp32) {
     LATER_CHECK(simt_gemm_acc(b.st, n2, n1, n2, -1.f, A + n1, lda, A + n1, lda, 1, 1, A + n1 + n1 * lda, lda));
   } else {
     const Op16 x{xh, xl, ldx};
     LATER_CHECK(gemm(sub, 'N', 'T', n2, n2, n1, -1.f, x, x, 1.f, A + n1 + n1 * lda, lda, nullptr, nullptr, 0, 1));
   }
-  return potrf_rec(b, n2, A + n1 + n1 * lda, lda);
+  return potrf_rec(b, n2, A + n1 + n1 * lda, lda, col + n1);
 }
 
 B3 make_b3(cudaStream_t st, const Options& o, float* work, int64_t lwork, void* hwork, int64_t lhwork) {
@@ -704,8 +928,11 @@ int64_t rtrmm_hwork(int m, int n, const Options& o) {
   return (round_up(m, 8) * n + round_up(h, 8) * h + 1024) * mult(o);
 }
 int64_t rpotrf_hwork(int n, const Options& o) {
+  (void)o;
+  // the diagonal blocks' inverses (hi + lo), then the recursion's operand copies in the widest format (SPLIT3)
   const int64_t h = n / 2 + 64;
-  return (round_up(h, 8) * h + round_up(h / 2 + 64, 8) * (h / 2 + 64) + 2048) * mult(o);
+  const int64_t inv = 2 * inv_slots(n) * kInvSlot + 256;
+  return inv + (round_up(h, 8) * h + 2 * round_up(h / 2 + 64, 8) * (h / 2 + 64) + round_up(h, 8) * NB + 4096) * 2;
 }
 int64_t splitk_work() { return static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 256; }
 
@@ -786,6 +1013,21 @@ later_status_t rpotrf(cudaStream_t st, char uplo, int n, float* A, int64_t lda, 
   if (n > NB && (!hwork || lhwork < rpotrf_hwork(n, o) || (reinterpret_cast<uintptr_t>(hwork) & 15)))
     return LATER_ERR_WORKSPACE;
   B3 b = make_b3(st, o, work, lwork, hwork, lhwork);
+  if (n > NB) {
+    // inverses of the factor's diagonal blocks first in hwork; the recursion's scratch after them
+    b.tc_small = true;
+    b.leaf_gemm = o.prec != LATER_PREC_SPLIT3;  // SPLIT3 keeps FP32 substitution in the block solves
+    const int64_t slots = inv_slots(n) * kInvSlot;
+    if (b.leaf_gemm) {
+      b.inv_hi = static_cast<__half*>(hwork);
+      b.inv_lo = b.inv_hi + slots;
+    }
+    const size_t skip = static_cast<size_t>(2 * slots) * 2;
+    b.h += skip;
+    b.hcap = b.hcap > skip ? b.hcap - skip : 0;
+  }
+  std::vector<char> done(static_cast<size_t>(inv_slots(std::max(n, 1))), 0);
+  b.inv_done = &done;
   return potrf_rec(b, n, A, lda);
 }
 
