@@ -733,10 +733,15 @@ def spd_result(a, n, kappa, precision, steps, warmup, cpu=True, ref=None):
     solve_s = time.perf_counter() - t0
     flops = n ** 3 / 3.0
     peak = _peaks().get("bf16_tflops") or 1900.0
-    ach = flops / fact_ms / 1e9
+    # the factorisation is ~1800 small launches: replayed from a captured CUDA graph (the way to run it on
+    # GB300 when it is repeated) it is reported as the value; the direct call is beside it
+    best_ms = graph_ms if isinstance(graph_ms, float) else fact_ms
+    ach = flops / best_ms / 1e9
     out = {"workload": f"rpotrf n={n} SPD kappa={kappa:g} ({precision} tensor-core updates) + FP64 refinement, "
                        f"{k} RHS to backward error 1e-12",
-           "value": ach, "unit": "TFLOP/s (n^3/3)", "ms_per_step": fact_ms, "steps": steps,
+           "value": ach, "unit": "TFLOP/s (n^3/3)", "ms_per_step": best_ms,
+           "timed_as": "CUDA graph replay" if isinstance(graph_ms, float) else "direct call",
+           "direct_call": {"ms_per_step": fact_ms, "value": flops / fact_ms / 1e9}, "steps": steps,
            "factor_status": st, "solve": {"seconds_incl_factor": solve_s, **info},
            "graph_replay": ({"ms_per_step": graph_ms, "value": flops / graph_ms / 1e9}
                             if isinstance(graph_ms, float) else graph_ms),

@@ -14,6 +14,12 @@
 //     the diagonal exit at once), alpha / beta in the epilogue;
 //   * the leaves are FP32 kernels of this file (substitution TRSM, TRMM, and a
 //     one-CTA Cholesky with a pivot check that reports LATER_ERR_NUMERIC);
+//   * in rpotrf, the parts the reference runs in FP32 (updates below its
+//     cuSOLVER / cublasStrsm block sizes) run as SPLIT3 tensor-core products
+//     (hi + lo operands, FP32-level), and the triangular solves with at least
+//     kInvMinRows rows are products with the inverse of the factor's 128-column
+//     diagonal block, inverted once, all blocks of a node in one launch
+//     (trtri_blocks_kernel); smaller solves keep the FP32 substitution leaf;
 //   * rtrmm adds L21 B1 into C2 in the GEMM epilogue (beta = 1): no tempC;
 //   * 16-bit operand copies are written by the producing leaf (solved X) or
 //     converted once per operand block right before its GEMM;
