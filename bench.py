@@ -458,6 +458,36 @@ def run_ours(a, rank, world, local_rank):
         else:
             same_gpu = {"unavailable": "oracle/_ref not built"}
 
+    # ---- the same QR replayed from a captured CUDA graph (launch overhead of the direct call)
+    graph_replay = None
+    try:
+        cs = torch.cuda.Stream()
+        cs.wait_stream(st)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(cs):
+            A.copy_(A0)
+            lg.later_rgsqrf(A, R, work, hwork, precision=a.precision, cgs2=a.cgs2, leaf=a.leaf, panel=a.panel,
+                            stream=cs)
+            torch.cuda.synchronize()
+            with torch.cuda.graph(graph, stream=cs):
+                lg.later_rgsqrf(A, R, work, hwork, precision=a.precision, cgs2=a.cgs2, leaf=a.leaf,
+                                panel=a.panel, stream=cs)
+        gts = []
+        for _ in range(a.steps):
+            A.copy_(A0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            graph.replay()
+            e1.record(st)
+            torch.cuda.synchronize()
+            gts.append(e0.elapsed_time(e1))
+        gms = statistics.median(gts)
+        graph_replay = {"ms_per_step": gms, "value": flops / gms / 1e9, "unit": "TFLOP/s"}
+        del graph
+    except Exception as e:  # noqa: BLE001
+        graph_replay = {"error": f"{type(e).__name__}: {e}"}
+
     # ---- per-class trace of one extra step (roofline of the dominant kernel)
     A.copy_(A0)
     lg.trace_begin()
@@ -583,7 +613,7 @@ def run_ours(a, rank, world, local_rank):
                                      "FP32 checker's own rounding)", "seconds": t_acc},
             "executed_tflops": 2.0 * m * n * n / ms_step / 1e9, "alt_precision": alt,
             "roofline": roof, "roofline_gemm": roof_gemm, "cpu_baseline": cpu, "e2e": e2e,
-            "same_gpu_comparators": same_gpu, "gpu_launches": launches,
+            "same_gpu_comparators": same_gpu, "graph_replay": graph_replay, "gpu_launches": launches,
             "launches_per_step": launches / max(1, a.steps), "clocks": clocks,
             "wall_s_timed_region": t_wall,
             "trace_ms": {"gemm": tr["gemm_ms"], "panel": tr["panel_ms"], "leaf_gemm": tr["leaf_gemm_ms"],
