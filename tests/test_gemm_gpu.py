@@ -74,6 +74,26 @@ def test_gemm_splitk_deterministic(cuda):
     assert torch.equal(D1, D2)
 
 
+@pytest.mark.parametrize("m,n,k,beta", [(128, 128, 16384, 0.0), (256, 384, 8192, 1.0), (200, 136, 12000, 1.0),
+                                         (1024, 512, 4096, 0.0)])
+def test_gemm_splitk_alpha_beta_ragged(cuda, m, n, k, beta):
+    """Split-K (partial tiles in `work`, reduced in a fixed order by a second launch) with alpha, beta C and
+    ragged tile edges: FP64 check and bit-for-bit repeatable."""
+    g = torch.Generator(device="cuda").manual_seed(m + n + k)
+    A = _operand(k, m, torch.float16, gen=g)
+    B = _operand(k, n, torch.float16, gen=g)
+    C = lg.colmajor(torch.randn(m, n, generator=g, device="cuda"))
+    work = torch.empty(1 << 24, dtype=torch.float32, device="cuda")
+    outs = []
+    for _ in range(2):
+        outs.append(lg.gemm16("T", "N", A, B, alpha=0.5, beta=beta, C=C if beta else None, work=work))
+        assert lg.device_status() == 0
+    ref = _ref("T", "N", A, B, 0.5, beta, C)
+    err = (outs[0].double() - ref).norm() / ref.norm()
+    assert err < rel_tol(k), float(err)
+    assert torch.equal(outs[0], outs[1])
+
+
 def test_gemm_leading_dims(cuda):
     m, n, k = 300, 200, 136
     g = torch.Generator(device="cuda").manual_seed(3)

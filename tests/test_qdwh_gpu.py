@@ -39,7 +39,7 @@ def test_qdwh_polar_matches_lapack_and_oracle(cuda, m, n, kappa):
     U, H, it = lg.later_qdwh_polar(_dev(A))
     assert lg.device_status() == 0
     assert 1 <= it <= 6, it
-    orth, bwd = _check(A, U.cpu().numpy(), H.cpu().numpy(), kappa, 1e-4, 5e-6)
+    orth, bwd = _check(A, U.cpu().numpy(), H.cpu().numpy(), kappa, 1e-4, 1e-5)
     if m * n <= 1024 * 1024:
         Uo, Ho, it_o = lo.qdwh_polar(A)
         orth_o = np.linalg.norm(Uo.T.astype(np.float64) @ Uo - np.eye(n))
