@@ -34,6 +34,7 @@
 #include "blas3.cuh"
 #include "dense_dev.cuh"
 #include "panel.cuh"
+#include "ptx.cuh"
 #include "runtime.cuh"
 
 namespace later {
@@ -134,6 +135,8 @@ constexpr int XS = 132;   // shared-memory row stride of the X tile
 __global__ void __launch_bounds__(256) trsm_rlt_leaf(int m, int nb, int R, const float* __restrict__ L, int64_t ldl,
                                                      float* B, int64_t ldb, void* xh, void* xl, int64_t ldh,
                                                      int mode) {
+  griddep_wait();  // inputs come from the previous kernel in the stream
+  griddep_launch();
   extern __shared__ __align__(16) float sm[];
   float* Lc = sm;             // L[j][l] at l*LDL + j; diagonal blocks replaced by their inverses
   float* Xs = sm + LDL * NB;  // X[r][c] at r*XS + c
@@ -249,6 +252,8 @@ __global__ void __launch_bounds__(256) trsm_rlt_leaf(int m, int nb, int R, const
 // lane updates its rows below k. L is staged column-major (stride 129).
 __global__ void __launch_bounds__(256) trsm_lln_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl, float* B,
                                                      int64_t ldb, void* xh, void* xl, int64_t ldh, int mode) {
+  griddep_wait();  // inputs come from the previous kernel in the stream
+  griddep_launch();
   extern __shared__ __align__(16) float sm[];
   float* Lc = sm;  // L[i][k] at i + k*129
   stage_lower(nb, L, ldl, Lc, 1, 129);
@@ -291,6 +296,8 @@ __global__ void __launch_bounds__(256) trsm_lln_leaf(int nb, int n, const float*
 // (stride 129) so that row k of L, which multiplies x_k, is contiguous.
 __global__ void __launch_bounds__(256) trsm_llt_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl, float* B,
                                                      int64_t ldb) {
+  griddep_wait();  // inputs come from the previous kernel in the stream
+  griddep_launch();
   extern __shared__ __align__(16) float sm[];
   float* Lr = sm;  // L[k][i] at k*129 + i
   stage_lower(nb, L, ldl, Lr, 129, 1);
@@ -329,6 +336,8 @@ __global__ void __launch_bounds__(256) trsm_llt_leaf(int nb, int n, const float*
 // per 64 columns; each thread accumulates 8 rows x 4 columns... of its share.
 __global__ void __launch_bounds__(256) trmm_leaf(int nb, int n, const float* __restrict__ L, int64_t ldl,
                                                  const float* __restrict__ B, int64_t ldb, float* C, int64_t ldc) {
+  griddep_wait();  // inputs come from the previous kernel in the stream
+  griddep_launch();
   extern __shared__ float sm[];
   float* Ls = sm;             // [i][k]
   float* Bs = sm + NB * 129;  // [k][c] at k*65 + c
@@ -467,6 +476,8 @@ struct PotrfSmem {
 };
 
 __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda, int* status) {
+  griddep_wait();  // inputs come from the previous kernel in the stream
+  griddep_launch();
   extern __shared__ __align__(16) float sm[];
   float* Ac = sm;  // A[i][j] at j*LDL + i (lower triangle used)
   PotrfSmem& ps = *reinterpret_cast<PotrfSmem*>(sm + LDL * NB);
@@ -544,6 +555,8 @@ struct InvBlocks {
 
 __global__ void __launch_bounds__(256) trtri_blocks_kernel(const float* __restrict__ L, int64_t ldl, InvBlocks blocks,
                                                            __half* vh_tab, __half* vl_tab) {
+  griddep_wait();  // inputs come from the previous kernel in the stream
+  griddep_launch();
   extern __shared__ __align__(16) float sm[];
   float* Lc = sm;
   float* V = sm + LDL * NB;
@@ -704,7 +717,8 @@ later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float*
     TraceScope tr(b.st, TRACE_OTHER);
     // 64 rows per CTA while that still gives two CTAs per SM, else 32
     const int R = (m + 63) / 64 >= 2 * num_sms() ? 64 : 32;
-    trsm_rlt_leaf<<<(m + R - 1) / R, 256, smem, b.st>>>(m, n, R, L, ldl, B, ldb, xh, xl, ldh, mode_of(b.o.prec));
+    LATER_CHECK_CUDA(launch_pdl(trsm_rlt_leaf, dim3((m + R - 1) / R), dim3(256), smem, b.st, m, n, R, L, ldl, B, ldb,
+                                xh, xl, ldh, mode_of(b.o.prec)));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -747,7 +761,8 @@ later_status_t trsm_lln(B3& b, int m, int n, const float* L, int64_t ldl, float*
     const size_t smem = NB * 129 * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(trsm_lln_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_OTHER);
-    trsm_lln_leaf<<<(n + 7) / 8, 256, smem, b.st>>>(m, n, L, ldl, B, ldb, xh, xl, ldh, mode_of(b.o.prec));
+    LATER_CHECK_CUDA(launch_pdl(trsm_lln_leaf, dim3((n + 7) / 8), dim3(256), smem, b.st, m, n, L, ldl, B, ldb, xh, xl, ldh,
+                                mode_of(b.o.prec)));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -778,7 +793,7 @@ later_status_t trsm_llt(B3& b, int m, int n, const float* L, int64_t ldl, float*
     const size_t smem = NB * 129 * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(trsm_llt_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_OTHER);
-    trsm_llt_leaf<<<(n + 7) / 8, 256, smem, b.st>>>(m, n, L, ldl, B, ldb);
+    LATER_CHECK_CUDA(launch_pdl(trsm_llt_leaf, dim3((n + 7) / 8), dim3(256), smem, b.st, m, n, L, ldl, B, ldb));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -810,7 +825,7 @@ later_status_t trmm_rec(B3& b, int m, int n, const float* L, int64_t ldl, const 
     const size_t smem = (NB * 129 + NB * 65) * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(trmm_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_OTHER);
-    trmm_leaf<<<(n + 63) / 64, 256, smem, b.st>>>(m, n, L, ldl, B, ldb, C, ldc);
+    LATER_CHECK_CUDA(launch_pdl(trmm_leaf, dim3((n + 63) / 64), dim3(256), smem, b.st, m, n, L, ldl, B, ldb, C, ldc));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -853,7 +868,7 @@ later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
     const size_t smem = kPotrfLeafSmem;
     if (!smem_attr(reinterpret_cast<const void*>(potrf_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_PANEL);
-    potrf_leaf<<<1, 256, smem, b.st>>>(n, A, lda, device_status_ptr());
+    LATER_CHECK_CUDA(launch_pdl(potrf_leaf, dim3(1), dim3(256), smem, b.st, n, A, lda, device_status_ptr()));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -866,7 +881,8 @@ later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
     if (blk.n > 0) {
       if (!smem_attr(reinterpret_cast<const void*>(trtri_blocks_kernel), kTrtriSmem)) return LATER_ERR_CUDA;
       // A points at the diagonal block starting at column `col`; the kernel takes the factor's origin
-      trtri_blocks_kernel<<<blk.n, 256, kTrtriSmem, b.st>>>(A - col - col * lda, lda, blk, b.inv_hi, b.inv_lo);
+      LATER_CHECK_CUDA(launch_pdl(trtri_blocks_kernel, dim3(blk.n), dim3(256), kTrtriSmem, b.st,
+                                  static_cast<const float*>(A - col - col * lda), lda, blk, b.inv_hi, b.inv_lo));
       note_launch();
       LATER_CHECK_CUDA(cudaGetLastError());
     }

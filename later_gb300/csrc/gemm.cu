@@ -207,7 +207,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   const int kb1 = min(kb0 + p.kb_per_split, p.kb_total);
   const int nkb = kb1 - kb0;
   // Lower-triangular output (SYRK): a tile entirely above the diagonal has no work.
-  if (p.lower && m0 + BM - 1 < n0 + p.diag) return;
+  if (p.lower && m0 + BM - 1 < n0 + p.diag) {
+    griddep_wait();
+    return;
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -222,6 +225,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   if (warp == 1) tmem_alloc(tmem_slot, C_::TMEM_COLS);
   tc_fence_before();
   __syncthreads();
+  griddep_wait();  // operands and C are written by the previous kernel in the stream
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
@@ -329,6 +333,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   // --------------------------------------------------------------- epilogue
   const bool drained = mbar_wait(done, 0, kDrainBudgetCycles);
   tc_fence_after();
+  griddep_launch();  // the next kernel's CTAs may be scheduled while this epilogue runs
   const bool ok = drained && (*abort_flag == 0) && nkb > 0;
   if (!ok && threadIdx.x == 0) report(p.status, DEV_TIMEOUT);
 
@@ -391,6 +396,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 template <int BN>
 __global__ void __launch_bounds__(256) splitk_reduce_kernel(const GemmArgs p) {
   __shared__ float part[8][4][33];
+  griddep_wait();
   const int tiles_per_row_groups = (BM / 32) * (BN / 4);
   const int tile = blockIdx.x / tiles_per_row_groups;
   const int rem = blockIdx.x % tiles_per_row_groups;
@@ -496,6 +502,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  griddep_wait();  // operands and C are written by the previous kernel in the stream
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
@@ -547,6 +554,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
           }
         }
       }
+      griddep_launch();  // every load of this CTA is issued: the next kernel may be scheduled
       // Drain: every issued load must land before the CTA may exit.
       for (uint32_t j = (g > STAGES ? g - STAGES : 0); j < g; ++j)
         mbar_wait(&full[j % STAGES], (j / STAGES) & 1, kDrainBudgetCycles);
@@ -689,9 +697,8 @@ later_status_t launch_persistent(const CUtensorMap& a, const CUtensorMap& b, con
     LATER_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, P_::SMEM));
     attr_done[dev] = true;
   }
-  kern<<<ctas, kPersistThreads, P_::SMEM, st>>>(a, b, al, bl, args);
+  LATER_CHECK_CUDA(launch_pdl(kern, dim3(ctas), dim3(kPersistThreads), P_::SMEM, st, a, b, al, bl, args));
   note_launch();
-  LATER_CHECK_CUDA(cudaGetLastError());
   return LATER_OK;
 }
 
@@ -733,14 +740,12 @@ later_status_t launch_cfg(const CUtensorMap& a, const CUtensorMap& b, const CUte
     LATER_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C_::SMEM));
     attr_done[dev] = true;
   }
-  kern<<<grid, kGemmThreads, C_::SMEM, st>>>(a, b, al, bl, args);
+  LATER_CHECK_CUDA(launch_pdl(kern, grid, dim3(kGemmThreads), C_::SMEM, st, a, b, al, bl, args));
   note_launch();
-  LATER_CHECK_CUDA(cudaGetLastError());
   if (args.splits > 1) {
     const int blocks = static_cast<int>(grid.x) * (BM / 32) * (BN / 4);
-    splitk_reduce_kernel<BN><<<blocks, 256, 0, st>>>(args);
+    LATER_CHECK_CUDA(launch_pdl(splitk_reduce_kernel<BN>, dim3(blocks), dim3(256), 0, st, args));
     note_launch();
-    LATER_CHECK_CUDA(cudaGetLastError());
   }
   return LATER_OK;
 }

@@ -88,6 +88,14 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 
+// Programmatic dependent launch. A kernel launched with launch_pdl (runtime.cuh) may be scheduled while
+// the previous kernel in its stream is still running: griddep_wait() blocks until that kernel has
+// completed and its writes are visible, so every CTA calls it before its first global access (read or
+// write). griddep_launch() lets the next such kernel be scheduled before this one ends. Both are no-ops
+// in a kernel launched without the attribute.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
+#include <utility>
 #include "status.cuh"
 
 namespace later {
@@ -131,5 +132,25 @@ class TraceScope {
 };
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+// Programmatic dependent launch, on unless LATER_PDL=0: the kernel may be scheduled before the previous
+// kernel in `st` has ended (its prologue overlaps that kernel's tail), so it must call griddep_wait()
+// (ptx.cuh) in every CTA before its first global access.
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 }  // namespace later

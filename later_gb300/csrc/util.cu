@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cstdlib>
 
 #include "ptx.cuh"
 #include "runtime.cuh"
@@ -62,11 +63,21 @@ int num_sms() {
   return v;
 }
 
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("LATER_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 namespace {
 
 // Each thread converts 4 consecutive rows of one column.
 __global__ void convert_kernel(int m, int n, const float* __restrict__ A, int64_t lda, void* hi, void* lo,
                                int64_t ldh, int mode, int* status) {
+  griddep_wait();  // inputs come from the previous kernel in the stream
+  griddep_launch();
   const int col = blockIdx.y * blockDim.y + threadIdx.y;
   const int r0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
   if (col >= n || r0 >= m) return;
@@ -209,7 +220,7 @@ later_status_t convert16(cudaStream_t st, int m, int n, const float* A, int64_t 
     return LATER_OK;
   }
   TraceScope trace(st, TRACE_OTHER);
-  convert_kernel<<<grid, block, 0, st>>>(m, n, A, lda, hi, lo, ldh, prec, device_status_ptr());
+  LATER_CHECK_CUDA(launch_pdl(convert_kernel, grid, block, 0, st, m, n, A, lda, hi, lo, ldh, prec, device_status_ptr()));
   note_launch();
   return cuda_status(cudaGetLastError());
 }
