@@ -15,8 +15,11 @@ per-step events). `value` is the device-timed rate with inputs resident in
 HBM; `e2e` is the same QR through the public API with the matrix copied from
 pinned host memory and Q and R copied back inside the timed region.
 
---impl reference times the reference algorithm on the host cores: the
-oracle's numpy restatement of later_rgsqrf (no GPU), on a bounded sample.
+--impl reference times the reference LATER's own rgsqrf on the same GPU and
+matrix (its kernels compiled from its sources into oracle/_ref, its host
+recursion restated with the same cuBLAS calls), device time and end to end
+with plain memcpys around the call; where oracle/_ref is not built, the
+oracle's numpy restatement on the host cores, on a bounded sample.
 
 Multi-GPU: a single QR does not shard (replicas only); under torchrun every
 rank factors its own matrix and `value` sums the ranks' rates (weak scaling).
@@ -192,6 +195,15 @@ def host_sgeqrf_rate(m, n, seed):
     return qr_flops(m, n) / dt / 1e12, dt
 
 
+def flat(t):
+    """The storage of a column-major (m x n, strides (1, m)) tensor as one contiguous vector: copies
+    between such host and device tensors then run as single plain memcpys (about 200 GB/s each way on
+    GB300), where copy_ on the transposed views takes a several times slower strided path."""
+    v = t.t()
+    assert v.is_contiguous()
+    return v.reshape(-1)
+
+
 def time_reference_gpu(a, A0, ref, steps, warmup, clocks=False):
     """The reference LATER's rgsqrf on this GPU (oracle/_ref: its kernels compiled from its sources,
     its host recursion restated call for call with the same cuBLAS calls) on the device matrix A0:
@@ -235,10 +247,10 @@ def time_reference_gpu(a, A0, ref, steps, warmup, clocks=False):
     e0.record(st)
     k = max(1, min(steps, 3))
     for _ in range(k):
-        A.copy_(hA, non_blocking=True)
+        flat(A).copy_(flat(hA), non_blocking=True)
         ref.rgsqrf(A, R, work, hwork)
-        hQ.copy_(A, non_blocking=True)
-        hR.copy_(R, non_blocking=True)
+        flat(hQ).copy_(flat(A), non_blocking=True)
+        flat(hR).copy_(flat(R), non_blocking=True)
     e1.record(st)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / k
@@ -528,13 +540,24 @@ def run_ours(a, rank, world, local_rank):
         torch.cuda.synchronize()
         e0.record(st)
         for _ in range(a.e2e_steps):
-            A.copy_(hA, non_blocking=True)
+            flat(A).copy_(flat(hA), non_blocking=True)
             qr()
-            hQ.copy_(A, non_blocking=True)
-            hR.copy_(R, non_blocking=True)
+            flat(hQ).copy_(flat(A), non_blocking=True)
+            flat(hR).copy_(flat(R), non_blocking=True)
         e1.record(st)
         torch.cuda.synchronize()
         e2e["serial_copies_ms_per_step"] = e0.elapsed_time(e1) / a.e2e_steps
+        # this host's pinned copy bandwidth (1 GiB each way, contiguous): the floor the copies sit on
+        flat_d, flat_h = flat(A), flat(hQ)
+        bw = {}
+        for name, dst, src in (("h2d", flat_d, flat(hA)), ("d2h", flat_h, flat_d)):
+            torch.cuda.synchronize()
+            e0.record(st)
+            dst.copy_(src, non_blocking=True)
+            e1.record(st)
+            torch.cuda.synchronize()
+            bw[name] = flat_d.numel() * 4 / (e0.elapsed_time(e1) * 1e6)
+        e2e["pinned_copy_gbs"] = bw
 
     if same_gpu and e2e and "reference_rgsqrf" in same_gpu:
         same_gpu["e2e_speedup_vs_reference"] = same_gpu["reference_rgsqrf"]["e2e_ms"] / e2e["ms_per_step"]

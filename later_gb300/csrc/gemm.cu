@@ -36,6 +36,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <mutex>
 
@@ -810,16 +811,25 @@ later_status_t tc_gemm(const GemmCall& g, const Scratch& s, cudaStream_t st, lon
   const int tiles = tiles_m * tiles_n;
   const int kb_total = (g.K + BK - 1) / BK;
 
-  // Split-K when the tile grid leaves SMs idle; at least 4 K blocks per split.
+  // Split-K when the tile grid leaves SMs idle: the split count that minimises (waves of CTAs) x (K
+  // blocks per split + a fixed cost of 8 K blocks per CTA for its prologue and partial tile), with at
+  // least 4 K blocks per split and the fewest splits on a tie (one CTA per SM: a split count that
+  // spills a few CTAs into a second wave doubles the time).
   int splits = 1;
   if (tiles < nsm && s.partial) {
-    int want = (nsm + tiles - 1) / tiles;
-    int maxk = kb_total / 4;
-    splits = want < maxk ? want : maxk;
+    constexpr int64_t kCtaCost = 8;
     const int64_t per = static_cast<int64_t>(tiles) * BM * BN;
     const int64_t fit = per > 0 ? s.partial_floats / per : 0;
-    if (splits > fit) splits = static_cast<int>(fit);
-    if (splits < 1) splits = 1;
+    const int smax = static_cast<int>(std::min<int64_t>(kb_total / 4, fit));
+    int64_t best = kb_total + kCtaCost;  // one split, one wave
+    for (int c = 2; c <= smax; ++c) {
+      const int64_t waves = (static_cast<int64_t>(tiles) * c + nsm - 1) / nsm;
+      const int64_t cost = waves * ((kb_total + c - 1) / c + kCtaCost);
+      if (cost < best) {
+        best = cost;
+        splits = c;
+      }
+    }
   }
   int kb_per_split = (kb_total + splits - 1) / splits;
   splits = (kb_total + kb_per_split - 1) / kb_per_split;

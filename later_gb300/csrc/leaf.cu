@@ -41,6 +41,7 @@
 
 #include "dense_dev.cuh"
 #include "leaf.cuh"
+#include "ptx.cuh"
 #include "tsqr_dev.cuh"
 
 namespace later {
@@ -1362,6 +1363,7 @@ __global__ void __launch_bounds__(LT, 1) leaf_res_kernel(LeafPlan P) {
     }
   }
   __syncthreads();
+  griddep_launch();  // the next kernel (a trailing update) may be scheduled as these CTAs finish
   if (ok) res_store(P, S.X, r0, rows, 0, P.w, true);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1397,6 +1399,7 @@ __global__ void __launch_bounds__(LT, 1) leaf_kernel(LeafPlan P) {
   }
   // Exit protocol: the last CTA out resets the counters for the next launch.
   __syncthreads();
+  griddep_launch();
   if (threadIdx.x == 0) {
     __threadfence();
     const int prev = atomicAdd(P.sync + 1, 1);
