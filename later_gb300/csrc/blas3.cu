@@ -708,7 +708,7 @@ later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float*
     g.out.Dl = xl;
     g.out.ldh = ldh;
     g.prec = LATER_PREC_SPLIT3;
-    g.out_prec = b.o.prec;
+    g.out_prec = xl ? LATER_PREC_SPLIT3 : b.o.prec;  // with xl: X's copy as a hi + lo pair
     return tc_gemm(g, sub.sc, b.st, b.o.budget);
   }
   if (n <= NB) {
@@ -718,7 +718,7 @@ later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float*
     // 64 rows per CTA while that still gives two CTAs per SM, else 32
     const int R = (m + 63) / 64 >= 2 * num_sms() ? 64 : 32;
     LATER_CHECK_CUDA(launch_pdl(trsm_rlt_leaf, dim3((m + R - 1) / R), dim3(256), smem, b.st, m, n, R, L, ldl, B, ldb,
-                                xh, xl, ldh, mode_of(b.o.prec)));
+                                xh, xl, ldh, xl ? 2 : mode_of(b.o.prec)));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -729,11 +729,13 @@ later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float*
     // FP32-level: both operands freshly split into SPLIT3 pairs
     B3 sub = b;
     sub.o.prec = LATER_PREC_SPLIT3;
-    Op16 x1, l21;
+    Op16 x1{xh, xl, ldh}, l21;  // X1's hi + lo pair, written by its solve, when the caller keeps one
     size_t used = 0;
-    LATER_CHECK(copy16(sub, m, n1, B, ldb, &x1, &used));
-    sub.h += used;
-    sub.hcap -= used;
+    if (!xh || !xl) {
+      LATER_CHECK(copy16(sub, m, n1, B, ldb, &x1, &used));
+      sub.h += used;
+      sub.hcap -= used;
+    }
     LATER_CHECK(copy16(sub, n2, n1, L + n1, ldl, &l21, &used));
     sub.h += used;
     sub.hcap -= used;
@@ -888,12 +890,18 @@ later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
     }
   }
   const bool fp32 = n <= kFp32Potrf;
-  // A21 <- A21 L11^{-T}; its 16-bit copy is written by the solve.
+  // A21 <- A21 L11^{-T}; its 16-bit copy is written by the solve. With FP16 (or SPLIT3) operands and
+  // the SPLIT3 small updates, the copy is a hi + lo pair (its hi is the FP16 copy), so the SPLIT3 updates
+  // of the solve and the syrk below the FP32 thresholds read it instead of converting A21 again.
+  const bool pair = b.tc_small && b.o.prec != LATER_PREC_BF16;
+  const bool keep = !fp32 || pair;
   const int64_t ldx = round_up(n2, 8);
   size_t used = 0;
-  char* xh = fp32 ? nullptr : take16(b, ldx * n1, &used);
-  if (!fp32 && !xh) return LATER_ERR_WORKSPACE;
-  char* xl = (xh && b.o.prec == LATER_PREC_SPLIT3) ? xh + ldx * n1 * 2 : nullptr;
+  B3 wide = b;
+  if (pair) wide.o.prec = LATER_PREC_SPLIT3;  // sizes the pair
+  char* xh = keep ? take16(wide, ldx * n1, &used) : nullptr;
+  if (keep && !xh) return LATER_ERR_WORKSPACE;
+  char* xl = (xh && (pair || b.o.prec == LATER_PREC_SPLIT3)) ? xh + ldx * n1 * 2 : nullptr;
   B3 sub = b;
   sub.h += used;
   sub.hcap -= used;
@@ -902,11 +910,13 @@ later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
   if (fp32 && b.tc_small) {
     B3 s3 = sub;
     s3.o.prec = LATER_PREC_SPLIT3;
-    Op16 x;
-    size_t u3 = 0;
-    LATER_CHECK(copy16(s3, n2, n1, A + n1, lda, &x, &u3));
-    s3.h += u3;
-    s3.hcap -= u3;
+    Op16 x{xh, xl, ldx};
+    if (!xh || !xl) {
+      size_t u3 = 0;
+      LATER_CHECK(copy16(s3, n2, n1, A + n1, lda, &x, &u3));
+      s3.h += u3;
+      s3.hcap -= u3;
+    }
     LATER_CHECK(gemm(s3, 'N', 'T', n2, n2, n1, -1.f, x, x, 1.f, A + n1 + n1 * lda, lda, nullptr, nullptr, 0, 1));
   } else if (fp32) {
     LATER_CHECK(simt_gemm_acc(b.st, n2, n1, n2, -1.f, A + n1, lda, A + n1, lda, 1, 1, A + n1 + n1 * lda, lda));
