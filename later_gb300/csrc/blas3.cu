@@ -461,11 +461,16 @@ __device__ void tri_inverse_smem(int nb, const float* Lc, int ldc, float* V, flo
 }
 
 // Lower Cholesky of an nb x nb block (nb <= 128) in one CTA, in shared memory
-// (column-major, stride LDL), right-looking over 32-column blocks. Warp 0
-// factors the 32 x 32 diagonal block with the compact register-window
-// Cholesky (dense_dev.cuh; pivots d * rsqrt(d)), one thread per row solves the
-// block column below it with the blocked row substitution, and the CTA
-// updates the trailing lower triangle in 4 x 4 register tiles. A non-positive
+// (column-major, stride LDL), right-looking over 32-column blocks with a
+// look-ahead of one block. Warp 0 factors the 32 x 32 diagonal block with the
+// compact register-window Cholesky (dense_dev.cuh; pivots d * rsqrt(d)) and
+// publishes its pivots eight at a time on named barriers; behind it, warps
+// 1..7 first apply the previous block's deferred update to the columns right
+// of this block, then solve the rows below this block (x R = a, eight columns
+// per published pivot group). After the block, the whole CTA updates only the
+// next block's columns, so the next Cholesky can start; the rest of the
+// update waits for it. Every entry receives the blocks' updates in block
+// order, each a 4 x 4-tiled sum over the block's 32 columns. A non-positive
 // (or NaN) pivot sets DEV_NUMERIC; the factorisation continues (with pivot 1)
 // so the kernel always finishes.
 struct PotrfSmem {
@@ -474,6 +479,47 @@ struct PotrfSmem {
   float rinv[32];
   int ok;
 };
+
+// Named barriers of potrf_leaf: one per pivot group of eight (kPotrfPub + g, counting all 256
+// threads: warp 0 arrives, the others wait).
+constexpr int kPotrfPub = 1;  // ids 1 .. 4
+
+// A[i][j] -= sum_{l < kb} A[i][k0 + l] A[j][k0 + l] for the lower-triangle entries j in [j0, j1), i in
+// [j, nb), in 4 x 4 tiles (j0 a multiple of 4), by threads t (of nthr) of the CTA.
+__device__ __forceinline__ void potrf_syrk(float* Ac, int nb, int k0, int kb, int j0, int j1, int t, int nthr) {
+  const int ncol = (j1 - j0 + 3) / 4;
+  // column tile c spans columns j0 + 4c .. + 3 and row tiles from row j0 + 4c to nb
+  int total = 0;
+  for (int c = 0; c < ncol; ++c) total += (nb - (j0 + 4 * c) + 3) / 4;
+  for (int q = t; q < total; q += nthr) {
+    int c = 0, rem = q;
+    for (;; ++c) {
+      const int nr = (nb - (j0 + 4 * c) + 3) / 4;
+      if (rem < nr) break;
+      rem -= nr;
+    }
+    const int c0 = j0 + 4 * c, i0 = c0 + 4 * rem;
+    float acc[4][4] = {};
+#pragma unroll 8
+    for (int l = 0; l < kb; ++l) {
+      const float4 a = *reinterpret_cast<const float4*>(&Ac[(k0 + l) * LDL + i0]);
+      const float4 b = *reinterpret_cast<const float4*>(&Ac[(k0 + l) * LDL + c0]);
+      const float av[4] = {a.x, a.y, a.z, a.w};
+      const float bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int i = i0 + u, j = c0 + v;
+        if (i < nb && j < j1 && j <= i) Ac[j * LDL + i] -= acc[u][v];
+      }
+  }
+}
 
 __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda, int* status) {
   griddep_wait();  // inputs come from the previous kernel in the stream
@@ -487,12 +533,25 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
   bool bad = false;
   for (int k0 = 0; k0 < nb; k0 += 32) {
     const int kb = min(32, nb - k0);
+    const int t0 = k0 + kb;  // first row below the block
     for (int e = tid; e < 32 * 32; e += blockDim.x) {
       const int i = e / 32, j = e % 32;
       ps.G[i * 33 + j] = (i < kb && j < kb && j <= i) ? Ac[(k0 + j) * LDL + k0 + i] : 0.f;
     }
     __syncthreads();
-    chol_upper(ps.G, kb, ps.Rc, ps.rinv, false, &ps.ok, 0.f);
+    if (tid < 32) {
+      chol_upper(ps.G, kb, ps.Rc, ps.rinv, false, &ps.ok, 0.f, kPotrfPub);
+    } else {
+      const int ct = tid - 32, nct = static_cast<int>(blockDim.x) - 32;
+      // the previous block's update of the columns right of this block (deferred to this phase; it
+      // touches neither this block's columns, which the solve below works on, nor the copy in G)
+      if (k0 > 0 && t0 < nb) potrf_syrk(Ac, nb, k0 - 32, 32, t0, nb, ct, nct);
+      // rows below the block: x R = a with R = L_D^T, eight columns per published pivot group
+      for (int b = 0; b < kb; b += 8) {
+        asm volatile("bar.sync %0, %1;" ::"r"(kPotrfPub + b / 8), "r"(static_cast<int>(blockDim.x)) : "memory");
+        for (int r = t0 + ct; r < nb; r += nct) rows_solve_group(Ac + k0 * LDL, LDL, kb, r, ps.Rc, ps.rinv, b);
+      }
+    }
     __syncthreads();
     if (!ps.ok) bad = true;
     // the factor back into the block: L[i][j] = R[j][i] = Rc[i * RCS + j]
@@ -500,40 +559,8 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
       const int i = e % kb, j = e / kb;
       if (j <= i) Ac[(k0 + j) * LDL + k0 + i] = ps.Rc[i * RCS + j];
     }
-    // rows below the diagonal block: x R = a with R = L_D^T
-    const int t0 = k0 + kb;
-    for (int r = t0 + tid; r < nb; r += blockDim.x) rows_solve(Ac + k0 * LDL, LDL, kb, r, ps.Rc, ps.rinv);
-    __syncthreads();
-    // trailing lower triangle: A[i][j] -= sum_l A[i][k0+l] A[j][k0+l], i >= j >= t0
-    const int t = nb - t0;
-    const int nt = (t + 3) / 4;
-    const int ntiles = nt * (nt + 1) / 2;
-    for (int q = tid; q < ntiles; q += blockDim.x) {
-      int ti = static_cast<int>((sqrtf(8.f * q + 1.f) - 1.f) * 0.5f);
-      while (ti * (ti + 1) / 2 > q) --ti;
-      while ((ti + 1) * (ti + 2) / 2 <= q) ++ti;
-      const int tj = q - ti * (ti + 1) / 2;
-      const int i0 = t0 + 4 * ti, j0 = t0 + 4 * tj;
-      float acc[4][4] = {};
-#pragma unroll 8
-      for (int l = 0; l < 32; ++l) {
-        const float4 a = *reinterpret_cast<const float4*>(&Ac[(k0 + l) * LDL + i0]);
-        const float4 b = *reinterpret_cast<const float4*>(&Ac[(k0 + l) * LDL + j0]);
-        const float av[4] = {a.x, a.y, a.z, a.w};
-        const float bv[4] = {b.x, b.y, b.z, b.w};
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const int i = i0 + u, j = j0 + v;
-          if (i < nb && j <= i) Ac[j * LDL + i] -= acc[u][v];
-        }
-    }
+    // this block's update of the next block's columns only; the rest waits for the next phase
+    if (t0 < nb) potrf_syrk(Ac, nb, k0, kb, t0, min(nb, t0 + 32), tid, blockDim.x);
     __syncthreads();
   }
   if (bad && tid == 0) report(status, DEV_NUMERIC);

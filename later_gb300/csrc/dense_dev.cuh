@@ -101,12 +101,12 @@ __device__ __forceinline__ void chol_upper(const float* G, int k, float* Rc, flo
   __syncwarp();
 }
 
-// x R = a for row r of the k columns X[c * ld + r], c < k, in place (R upper
-// k x k column-major in Rc, rinv its reciprocal pivots). Blocks of 8 columns:
-// the 8 x 8 diagonal block in registers, then the later columns in shared
-// memory, reading R as float4 pairs.
-__device__ __forceinline__ void rows_solve(float* X, int ld, int k, int r, const float* Rc, const float* rinv) {
-  for (int b = 0; b < k; b += 8) {
+// One eight-column group b of rows_solve: columns b .. b + 7 of row r are
+// solved (the 8 x 8 diagonal block in registers) and removed from the later
+// columns b + 8 .. k - 1 (R read as float4 pairs). Needs R's rows b .. b + 7.
+__device__ __forceinline__ void rows_solve_group(float* X, int ld, int k, int r, const float* Rc, const float* rinv,
+                                                 int b) {
+  {
     float x[8];
 #pragma unroll
     for (int l = 0; l < 8; ++l) x[l] = b + l < k ? X[(b + l) * ld + r] : 0.f;
@@ -137,6 +137,12 @@ __device__ __forceinline__ void rows_solve(float* X, int ld, int k, int r, const
       X[j * ld + r] = t;
     }
   }
+}
+
+// x R = a for row r of the k columns X[c * ld + r], c < k, in place (R upper
+// k x k column-major in Rc, rinv its reciprocal pivots), eight columns at a time.
+__device__ __forceinline__ void rows_solve(float* X, int ld, int k, int r, const float* Rc, const float* rinv) {
+  for (int b = 0; b < k; b += 8) rows_solve_group(X, ld, k, r, Rc, rinv, b);
 }
 
 }  // namespace
