@@ -132,9 +132,33 @@ __device__ __forceinline__ void stage_cols(int nb, const float* L, int64_t ldl, 
 // then the update of the columns after the block.
 constexpr int LDL = 132;  // shared-memory stride of staged L (16-byte aligned)
 constexpr int XS = 132;   // shared-memory row stride of the X tile
+
+// Column `lane` of D^-1 into y (zeros above the diagonal) for the w x w lower-triangular diagonal block D
+// starting at (cb, cb) of the column-major shared copy Lc (stride ldc), by forward substitution (one
+// warp: lane = column). The Cholesky leaf and the triangular-solve leaf share it, so an inverse kept by
+// the former is bit-identical to one the latter computes.
+__device__ __forceinline__ void tri_block_inverse_col(const float* Lc, int ldc, int cb, int w, int lane,
+                                                      float (&y)[32]) {
+#pragma unroll
+  for (int i = 0; i < 32; ++i) y[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    if (k < w) {
+      const float* dcol = Lc + (cb + k) * ldc + cb;  // column k of D
+      y[k] = y[k] / dcol[k];
+#pragma unroll
+      for (int i = k + 1; i < 32; ++i) y[i] -= dcol[i] * y[k];
+    }
+  }
+}
+
+// Table of the factor's 32 x 32 diagonal-block inverses (FP32), one slot per 32 columns: slot s holds
+// D_s^-1 column-major, entry (i, j) at s * kDinvSlot + j * 32 + i, zeros outside the block.
+constexpr int kDinvSlot = 32 * 32;
+
 __global__ void __launch_bounds__(256) trsm_rlt_leaf(int m, int nb, int R, const float* __restrict__ L, int64_t ldl,
                                                      float* B, int64_t ldb, void* xh, void* xl, int64_t ldh,
-                                                     int mode) {
+                                                     int mode, const float* __restrict__ dinv) {
   griddep_wait();  // inputs come from the previous kernel in the stream
   griddep_launch();
   extern __shared__ __align__(16) float sm[];
@@ -162,22 +186,27 @@ __global__ void __launch_bounds__(256) trsm_rlt_leaf(int m, int nb, int R, const
   __syncthreads();
   const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
   const int nblk = (nb + 31) / 32;
-  {
+  if (dinv) {
+    // the diagonal blocks' inverses, kept by the Cholesky leaf that factored L: whole 32 x 32 slots
+    // (zeros outside each block), four rows per float4, every load of a thread in flight at once
+    constexpr int kQ = 4 * kDinvSlot / 4 / 256;  // float4 per thread for four blocks
+    float4 v[kQ];
+#pragma unroll
+    for (int u = 0; u < kQ; ++u) {
+      const int q = threadIdx.x + u * 256;
+      v[u] = q < nblk * kDinvSlot / 4 ? __ldcg(reinterpret_cast<const float4*>(dinv) + q)
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kQ; ++u) {
+      const int q = threadIdx.x + u * 256, e = 4 * q;
+      const int blk = e / kDinvSlot, j = (e / 32) % 32, i = e % 32, cb = 32 * blk;
+      if (q < nblk * kDinvSlot / 4) *reinterpret_cast<float4*>(&Lc[(cb + j) * LDL + cb + i]) = v[u];
+    }
+  } else {
     float y[32];
     const int cb = warp * 32, w = min(32, nb - cb);
-    if (warp < nblk) {
-#pragma unroll
-      for (int i = 0; i < 32; ++i) y[i] = (i == lane) ? 1.f : 0.f;
-#pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        if (k < w) {
-          const float* dcol = Lc + (cb + k) * LDL + cb;  // column k of D
-          y[k] = y[k] / dcol[k];
-#pragma unroll
-          for (int i = k + 1; i < 32; ++i) y[i] -= dcol[i] * y[k];
-        }
-      }
-    }
+    if (warp < nblk) tri_block_inverse_col(Lc, LDL, cb, w, lane, y);
     __syncthreads();  // every read of the diagonal blocks is done
     if (warp < nblk && lane < w) {
 #pragma unroll
@@ -480,9 +509,10 @@ struct PotrfSmem {
   int ok;
 };
 
-// Named barriers of potrf_leaf: one per pivot group of eight (kPotrfPub + g, counting all 256
-// threads: warp 0 arrives, the others wait).
+// Named barriers of potrf_leaf: one per pivot group of eight (kPotrfPub + g, counting warps 0..6:
+// warp 0 arrives, warps 1..6 wait; warp 7 inverts the previous diagonal block meanwhile).
 constexpr int kPotrfPub = 1;  // ids 1 .. 4
+constexpr int kPotrfPubCount = 7 * 32;
 
 // A[i][j] -= sum_{l < kb} A[i][k0 + l] A[j][k0 + l] for the lower-triangle entries j in [j0, j1), i in
 // [j, nb), in 4 x 4 tiles (j0 a multiple of 4), by threads t (of nthr) of the CTA.
@@ -521,7 +551,16 @@ __device__ __forceinline__ void potrf_syrk(float* Ac, int nb, int k0, int kb, in
   }
 }
 
-__global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda, int* status) {
+// The w x w diagonal block at (cb, cb) of Ac, inverted by one warp into the table slot `out`.
+__device__ __forceinline__ void potrf_keep_inverse(const float* Ac, int cb, int w, float* out) {
+  const int lane = threadIdx.x & 31;
+  float y[32];
+  tri_block_inverse_col(Ac, LDL, cb, w, lane, y);
+#pragma unroll
+  for (int i = 0; i < 32; ++i) out[lane * 32 + i] = (lane < w && i < w) ? y[i] : 0.f;
+}
+
+__global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda, int* status, float* dinv) {
   griddep_wait();  // inputs come from the previous kernel in the stream
   griddep_launch();
   extern __shared__ __align__(16) float sm[];
@@ -540,16 +579,21 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
     }
     __syncthreads();
     if (tid < 32) {
-      chol_upper(ps.G, kb, ps.Rc, ps.rinv, false, &ps.ok, 0.f, kPotrfPub);
+      chol_upper(ps.G, kb, ps.Rc, ps.rinv, false, &ps.ok, 0.f, kPotrfPub, kPotrfPubCount);
     } else {
       const int ct = tid - 32, nct = static_cast<int>(blockDim.x) - 32;
+      // warp 7: the previous diagonal block's inverse into the table, for the triangular solves
+      if (tid >= kPotrfPubCount && k0 > 0 && dinv) potrf_keep_inverse(Ac, k0 - 32, 32, dinv + (k0 / 32 - 1) * kDinvSlot);
       // the previous block's update of the columns right of this block (deferred to this phase; it
       // touches neither this block's columns, which the solve below works on, nor the copy in G)
       if (k0 > 0 && t0 < nb) potrf_syrk(Ac, nb, k0 - 32, 32, t0, nb, ct, nct);
-      // rows below the block: x R = a with R = L_D^T, eight columns per published pivot group
-      for (int b = 0; b < kb; b += 8) {
-        asm volatile("bar.sync %0, %1;" ::"r"(kPotrfPub + b / 8), "r"(static_cast<int>(blockDim.x)) : "memory");
-        for (int r = t0 + ct; r < nb; r += nct) rows_solve_group(Ac + k0 * LDL, LDL, kb, r, ps.Rc, ps.rinv, b);
+      // rows below the block: x R = a with R = L_D^T, eight columns per published pivot group (warps 1..6)
+      if (tid < kPotrfPubCount) {
+        const int nsv = kPotrfPubCount - 32;
+        for (int b = 0; b < kb; b += 8) {
+          asm volatile("bar.sync %0, %1;" ::"r"(kPotrfPub + b / 8), "r"(kPotrfPubCount) : "memory");
+          for (int r = t0 + ct; r < nb; r += nsv) rows_solve_group(Ac + k0 * LDL, LDL, kb, r, ps.Rc, ps.rinv, b);
+        }
       }
     }
     __syncthreads();
@@ -564,6 +608,9 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
     __syncthreads();
   }
   if (bad && tid == 0) report(status, DEV_NUMERIC);
+  // the last diagonal block's inverse (warp 7), beside the store of the factor
+  const int klast = (nb - 1) / 32 * 32;
+  if (tid >= kPotrfPubCount && dinv) potrf_keep_inverse(Ac, klast, nb - klast, dinv + (klast / 32) * kDinvSlot);
   for (int e = tid; e < nb * nb; e += blockDim.x) {
     const int i = e % nb, j = e / nb;
     if (i >= j) A[i + static_cast<int64_t>(j) * lda] = Ac[j * LDL + i];
@@ -647,6 +694,9 @@ struct B3 {
   __half* inv_hi = nullptr;
   __half* inv_lo = nullptr;
   std::vector<char>* inv_done = nullptr;  // per slot: inverse already in the table
+  // Cholesky only: the factor's 32 x 32 diagonal-block inverses (FP32), kept by the Cholesky leaves for the
+  // triangular-solve leaves (slot = factor column / 32)
+  float* dinv = nullptr;
 };
 
 // Solves with at least this many rows use the diagonal block's inverse (its
@@ -655,6 +705,7 @@ constexpr int kInvMinRows = 2048;
 
 constexpr int64_t kInvSlot = 128 * 128;  // 16-bit elements per inverse block (ld 128)
 inline int64_t inv_slots(int n) { return (n + 63) / 64; }
+inline int64_t dinv_slots(int n) { return (n + 31) / 32; }
 
 // Takes `elems` 16-bit elements from the hwork scratch (256-byte aligned).
 char* take16(B3& b, int64_t elems, size_t* mark) {
@@ -744,8 +795,9 @@ later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float*
     TraceScope tr(b.st, TRACE_OTHER);
     // 64 rows per CTA while that still gives two CTAs per SM, else 32
     const int R = (m + 63) / 64 >= 2 * num_sms() ? 64 : 32;
+    const float* dinv = (b.dinv && col >= 0) ? b.dinv + (col / 32) * kDinvSlot : nullptr;
     LATER_CHECK_CUDA(launch_pdl(trsm_rlt_leaf, dim3((m + R - 1) / R), dim3(256), smem, b.st, m, n, R, L, ldl, B, ldb,
-                                xh, xl, ldh, xl ? 2 : mode_of(b.o.prec)));
+                                xh, xl, ldh, xl ? 2 : mode_of(b.o.prec), dinv));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -897,7 +949,8 @@ later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
     const size_t smem = kPotrfLeafSmem;
     if (!smem_attr(reinterpret_cast<const void*>(potrf_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_PANEL);
-    LATER_CHECK_CUDA(launch_pdl(potrf_leaf, dim3(1), dim3(256), smem, b.st, n, A, lda, device_status_ptr()));
+    float* dinv = b.dinv ? b.dinv + (col / 32) * kDinvSlot : nullptr;
+    LATER_CHECK_CUDA(launch_pdl(potrf_leaf, dim3(1), dim3(256), smem, b.st, n, A, lda, device_status_ptr(), dinv));
     note_launch();
     return cuda_status(cudaGetLastError());
   }
@@ -991,7 +1044,9 @@ int64_t rpotrf_hwork(int n, const Options& o) {
   // the diagonal blocks' inverses (hi + lo), then the recursion's operand copies in the widest format (SPLIT3)
   const int64_t h = n / 2 + 64;
   const int64_t inv = 2 * inv_slots(n) * kInvSlot + 256;
-  return inv + (round_up(h, 8) * h + 2 * round_up(h / 2 + 64, 8) * (h / 2 + 64) + round_up(h, 8) * NB + 4096) * 2;
+  const int64_t dinv = dinv_slots(n) * kDinvSlot * 2 + 256;  // FP32 entries, in 16-bit units
+  return inv + dinv +
+         (round_up(h, 8) * h + 2 * round_up(h / 2 + 64, 8) * (h / 2 + 64) + round_up(h, 8) * NB + 4096) * 2;
 }
 int64_t splitk_work() { return static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 256; }
 
@@ -1081,7 +1136,11 @@ later_status_t rpotrf(cudaStream_t st, char uplo, int n, float* A, int64_t lda, 
       b.inv_hi = static_cast<__half*>(hwork);
       b.inv_lo = b.inv_hi + slots;
     }
-    const size_t skip = static_cast<size_t>(2 * slots) * 2;
+    size_t skip = static_cast<size_t>(2 * slots) * 2;
+    // then the FP32 table of the 32 x 32 diagonal-block inverses (256-byte aligned)
+    const uintptr_t d = (reinterpret_cast<uintptr_t>(b.h) + skip + 255) & ~uintptr_t(255);
+    b.dinv = reinterpret_cast<float*>(d);
+    skip = (d - reinterpret_cast<uintptr_t>(b.h)) + static_cast<size_t>(dinv_slots(n)) * kDinvSlot * sizeof(float);
     b.h += skip;
     b.hcap = b.hcap > skip ? b.hcap - skip : 0;
   }

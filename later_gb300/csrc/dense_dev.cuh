@@ -25,12 +25,12 @@ constexpr int RCS = 36;  // stride of the column-major 32 x 32 R factors in shar
 // original diagonal, a non-finite value, or, with `near_identity`,
 // max |G - I| > 1/4.
 // With pub_bar >= 0, warp 0 also arrives on named barrier pub_bar + g
-// (counting blockDim.x threads) once pivots 8g .. 8g + 7 are final (R rows and
+// (counting pub_count threads, default blockDim.x) once pivots 8g .. 8g + 7 are final (R rows and
 // rinv published; the last group may be partial): ceil(k / 8) arrivals, one
 // per barrier id, so other warps can consume R block by block. Each id is
 // used once per call: the caller separates calls by a full-block barrier.
 __device__ __forceinline__ void chol_upper(const float* G, int k, float* Rc, float* rinv, bool near_identity,
-                                           int* okout, float ratio = 1e-4f, int pub_bar = -1) {
+                                           int* okout, float ratio = 1e-4f, int pub_bar = -1, int pub_count = 0) {
   if (threadIdx.x >= 32) return;
   const int lane = threadIdx.x;
   float* Lb = Rc;  // scratch for the published block columns reuses Rc's layout: Lb[lane * RCS + kb .. kb+3]
@@ -78,7 +78,9 @@ __device__ __forceinline__ void chol_upper(const float* G, int k, float* Rc, flo
     *reinterpret_cast<float4*>(&Lb[lane * RCS + kb]) = make_float4(l[0], l[1], l[2], l[3]);
     __syncwarp();
     if (pub_bar >= 0 && ((kb + 4) % 8 == 0 || kb + 4 >= k))
-      asm volatile("bar.arrive %0, %1;" ::"r"(pub_bar + kb / 8), "r"(static_cast<int>(blockDim.x)) : "memory");
+      asm volatile("bar.arrive %0, %1;" ::"r"(pub_bar + kb / 8),
+                   "r"(pub_count > 0 ? pub_count : static_cast<int>(blockDim.x))
+                   : "memory");
     // rank-4 update of the window columns kb + 4 .. and shift by four
 #pragma unroll
     for (int j = 4; j < 32; ++j) {
