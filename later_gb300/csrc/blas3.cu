@@ -90,20 +90,25 @@ __device__ __forceinline__ void stage_cols(int nb, const float* L, int64_t ldl, 
   const int T = blockDim.x;
   const bool vec = (reinterpret_cast<uintptr_t>(L) % 16 == 0) && (ldl % 4 == 0) && (nb % 4 == 0);
   if (vec) {
+    // (column, row quad) of element e: a shift when nq is a power of two (nb = 128: 32 quads), which
+    // spares the integer divisions that otherwise dominate this copy
     const int nq = nb / 4, total = nq * nb;
+    const bool pow2 = (nq & (nq - 1)) == 0;
+    const int sh = __ffs(nq) - 1;
     for (int base = threadIdx.x; base < total; base += 8 * T) {
       float4 v[8];
+      int off[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int e = base + u * T;
-        v[u] = e < total ? *reinterpret_cast<const float4*>(L + 4 * (e % nq) + static_cast<int64_t>(e / nq) * ldl)
+        const int c = pow2 ? e >> sh : e / nq, q = e - c * nq;
+        off[u] = 4 * q + c * ldc;
+        v[u] = e < total ? *reinterpret_cast<const float4*>(L + 4 * q + static_cast<int64_t>(c) * ldl)
                          : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = base + u * T;
-        if (e < total) *reinterpret_cast<float4*>(dst + 4 * (e % nq) + (e / nq) * ldc) = v[u];
-      }
+      for (int u = 0; u < 8; ++u)
+        if (base + u * T < total) *reinterpret_cast<float4*>(dst + off[u]) = v[u];
     }
   } else {
     const int total = nb * nb;
@@ -167,19 +172,19 @@ __global__ void __launch_bounds__(256) trsm_rlt_leaf(int m, int nb, int R, const
   const int row0 = blockIdx.x * R;
   stage_cols(nb, L, ldl, Lc, LDL);
   {
-    const int total = R * nb;
+    const int total = R * nb, shr = __ffs(R) - 1;  // R is 32 or 64
     for (int base = threadIdx.x; base < total; base += 8 * 256) {
       float v[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int e = base + u * 256;
-        const int r = e % R, c = e / R;
+        const int r = e & (R - 1), c = e >> shr;
         v[u] = (e < total && row0 + r < m) ? B[row0 + r + static_cast<int64_t>(c) * ldb] : 0.f;
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int e = base + u * 256;
-        if (e < total) Xs[(e % R) * XS + e / R] = v[u];
+        if (e < total) Xs[(e & (R - 1)) * XS + (e >> shr)] = v[u];
       }
     }
   }
@@ -599,9 +604,9 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
     __syncthreads();
     if (!ps.ok) bad = true;
     // the factor back into the block: L[i][j] = R[j][i] = Rc[i * RCS + j]
-    for (int e = tid; e < kb * kb; e += blockDim.x) {
-      const int i = e % kb, j = e / kb;
-      if (j <= i) Ac[(k0 + j) * LDL + k0 + i] = ps.Rc[i * RCS + j];
+    for (int e = tid; e < 32 * 32; e += blockDim.x) {
+      const int i = e & 31, j = e >> 5;
+      if (j <= i && i < kb) Ac[(k0 + j) * LDL + k0 + i] = ps.Rc[i * RCS + j];
     }
     // this block's update of the next block's columns only; the rest waits for the next phase
     if (t0 < nb) potrf_syrk(Ac, nb, k0, kb, t0, min(nb, t0 + 32), tid, blockDim.x);
@@ -611,10 +616,9 @@ __global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda,
   // the last diagonal block's inverse (warp 7), beside the store of the factor
   const int klast = (nb - 1) / 32 * 32;
   if (tid >= kPotrfPubCount && dinv) potrf_keep_inverse(Ac, klast, nb - klast, dinv + (klast / 32) * kDinvSlot);
-  for (int e = tid; e < nb * nb; e += blockDim.x) {
-    const int i = e % nb, j = e / nb;
-    if (i >= j) A[i + static_cast<int64_t>(j) * lda] = Ac[j * LDL + i];
-  }
+  // the factor back to A: a column per warp, lanes along its rows on and below the diagonal
+  for (int j = tid / 32; j < nb; j += blockDim.x / 32)
+    for (int i = j + (tid & 31); i < nb; i += 32) A[i + static_cast<int64_t>(j) * lda] = Ac[j * LDL + i];
 }
 
 // Inverses of diagonal blocks of a lower-triangular factor, one CTA per block
