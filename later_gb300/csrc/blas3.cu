@@ -142,6 +142,8 @@ constexpr int XS = 132;   // shared-memory row stride of the X tile
 // starting at (cb, cb) of the column-major shared copy Lc (stride ldc), by forward substitution (one
 // warp: lane = column). The Cholesky leaf and the triangular-solve leaf share it, so an inverse kept by
 // the former is bit-identical to one the latter computes.
+// Column k of D is read as float4 quads from the one holding row k (ldc and cb keep them 16-byte
+// aligned): a quarter of the shared-memory loads of element-wise reads.
 __device__ __forceinline__ void tri_block_inverse_col(const float* Lc, int ldc, int cb, int w, int lane,
                                                       float (&y)[32]) {
 #pragma unroll
@@ -149,10 +151,19 @@ __device__ __forceinline__ void tri_block_inverse_col(const float* Lc, int ldc, 
 #pragma unroll
   for (int k = 0; k < 32; ++k) {
     if (k < w) {
-      const float* dcol = Lc + (cb + k) * ldc + cb;  // column k of D
-      y[k] = y[k] / dcol[k];
+      const float4* dq = reinterpret_cast<const float4*>(Lc + (cb + k) * ldc + cb);  // column k of D
+      float d[32];
 #pragma unroll
-      for (int i = k + 1; i < 32; ++i) y[i] -= dcol[i] * y[k];
+      for (int q = k / 4; q < 8; ++q) {
+        const float4 v = dq[q];
+        d[4 * q] = v.x;
+        d[4 * q + 1] = v.y;
+        d[4 * q + 2] = v.z;
+        d[4 * q + 3] = v.w;
+      }
+      y[k] = y[k] / d[k];
+#pragma unroll
+      for (int i = k + 1; i < 32; ++i) y[i] -= d[i] * y[k];
     }
   }
 }
@@ -565,7 +576,7 @@ __device__ __forceinline__ void potrf_keep_inverse(const float* Ac, int cb, int 
   for (int i = 0; i < 32; ++i) out[lane * 32 + i] = (lane < w && i < w) ? y[i] : 0.f;
 }
 
-__global__ void __launch_bounds__(256) potrf_leaf(int nb, float* A, int64_t lda, int* status, float* dinv) {
+__global__ void __launch_bounds__(256, 1) potrf_leaf(int nb, float* A, int64_t lda, int* status, float* dinv) {
   griddep_wait();  // inputs come from the previous kernel in the stream
   griddep_launch();
   extern __shared__ __align__(16) float sm[];

@@ -546,20 +546,24 @@ __device__ void res_load(const LeafPlan& P, float* X, int r0, int rows, int cols
   const int zr = ((rows + 3) & ~3) - rows;
   for (int e = tid; e < zr * cols; e += LT) X[(e / zr) * XS + rows + e % zr] = 0.f;
   if (P.vec) {
-    const int nq = rows / 4, total = nq * cols;
-    for (int base = tid; base < total; base += 8 * LT) {
-      float4 v[8];
+    // a column per warp (eight columns in flight), lanes along its row quads (nq <= 64)
+    const int nq = rows / 4, warp = tid >> 5, lane = tid & 31;
+    for (int cb = warp; cb < cols; cb += 8 * (LT / 32)) {
+      for (int qb = 0; qb < nq; qb += 32) {
+        const int q = qb + lane;
+        float4 v[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = base + u * LT;
-        v[u] = e < total ? __ldcg(reinterpret_cast<const float4*>(P.A + r0 + 4 * (e % nq) +
-                                                                  static_cast<int64_t>(e / nq) * P.lda))
-                         : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
+        for (int u = 0; u < 8; ++u) {
+          const int c = cb + u * (LT / 32);
+          v[u] = (c < cols && q < nq)
+                     ? __ldcg(reinterpret_cast<const float4*>(P.A + r0 + 4 * q + static_cast<int64_t>(c) * P.lda))
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = base + u * LT;
-        if (e < total) *reinterpret_cast<float4*>(&X[(e / nq) * XS + 4 * (e % nq)]) = v[u];
+        for (int u = 0; u < 8; ++u) {
+          const int c = cb + u * (LT / 32);
+          if (c < cols && q < nq) *reinterpret_cast<float4*>(&X[c * XS + 4 * q]) = v[u];
+        }
       }
     }
     const int tr = rows - 4 * nq;
@@ -576,29 +580,21 @@ __device__ void res_load(const LeafPlan& P, float* X, int r0, int rows, int cols
 
 // Writes columns [c0, c0 + cols) of the slab back to A (and Q's 16-bit copy when `shadow`).
 __device__ void res_store(const LeafPlan& P, const float* X, int r0, int rows, int c0, int cols, bool shadow) {
-  const int tid = threadIdx.x;
-  if (P.vec) {
-    const int nq = rows / 4, total = nq * cols;
-    for (int e = tid; e < total; e += LT) {
-      const int c = c0 + e / nq, q = e % nq;
-      *reinterpret_cast<float4*>(P.A + r0 + 4 * q + static_cast<int64_t>(c) * P.lda) =
-          *reinterpret_cast<const float4*>(&X[c * XS + 4 * q]);
+  // a column per warp, lanes along its rows (row quads when vectorised)
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int c = c0 + warp; c < c0 + cols; c += LT / 32) {
+    if (P.vec) {
+      const int nq = rows / 4;
+      for (int q = lane; q < nq; q += 32)
+        *reinterpret_cast<float4*>(P.A + r0 + 4 * q + static_cast<int64_t>(c) * P.lda) =
+            *reinterpret_cast<const float4*>(&X[c * XS + 4 * q]);
+      for (int r = 4 * nq + lane; r < rows; r += 32) P.A[r0 + r + static_cast<int64_t>(c) * P.lda] = X[c * XS + r];
+    } else {
+      for (int r = lane; r < rows; r += 32) P.A[r0 + r + static_cast<int64_t>(c) * P.lda] = X[c * XS + r];
     }
-    const int tr = rows - 4 * nq;
-    for (int e = tid; e < tr * cols; e += LT) {
-      const int r = 4 * nq + e % tr, c = c0 + e / tr;
-      P.A[r0 + r + static_cast<int64_t>(c) * P.lda] = X[c * XS + r];
-    }
-  } else {
-    for (int e = tid; e < rows * cols; e += LT) {
-      const int r = e % rows, c = c0 + e / rows;
-      P.A[r0 + r + static_cast<int64_t>(c) * P.lda] = X[c * XS + r];
-    }
-  }
-  if (shadow && P.qh) {
-    for (int e = tid; e < rows * cols; e += LT) {
-      const int r = e % rows, c = c0 + e / rows;
-      put_shadow(P.qh, P.ql, r0 + r + static_cast<int64_t>(c) * P.ldh, X[c * XS + r], P.mode);
+    if (shadow && P.qh) {
+      for (int r = lane; r < rows; r += 32)
+        put_shadow(P.qh, P.ql, r0 + r + static_cast<int64_t>(c) * P.ldh, X[c * XS + r], P.mode);
     }
   }
 }
