@@ -652,10 +652,13 @@ __device__ void res_tn_emit(const float* Xa, int a0, int na, const float* Xb, in
     __syncthreads();
   else
     asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthr) : "memory");
+  // entry e is (e mod 4 nta, e div 4 nta): a shift and a mask when 4 nta is a power of two (na = 32)
+  const int w4 = 4 * nta, sh = __ffs(w4) - 1;
+  const bool p2 = (w4 & (w4 - 1)) == 0;
   for (int e = tid; e < npad; e += nthr) {
     float s = 0.f;
     for (int gg = 0; gg < groups; ++gg) s += gp[gg * npad + e];
-    emit(e % (4 * nta), e / (4 * nta), s);
+    emit(p2 ? (e & (w4 - 1)) : e % w4, p2 ? (e >> sh) : e / w4, s);
   }
 }
 
