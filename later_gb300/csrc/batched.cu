@@ -68,21 +68,25 @@ __device__ void stage(float* dst, const Item& it, int r0, int rows, int c0, int 
   const int rq = (rows + 3) & ~3;
   const bool vec = rows == rq && (it.lda % 4 == 0) && (reinterpret_cast<uintptr_t>(it.A) % 16 == 0);
   if (vec) {  // r0 is a multiple of CR, so every float4 is aligned
+    // (column, row quad) of element e: a shift when nq is a power of two (every full chunk), which
+    // spares the integer divisions that otherwise dominate the staging
     const int nq = rq / 4, total = nq * nc;
+    const bool p2 = (nq & (nq - 1)) == 0;
+    const int sh = __ffs(nq) - 1;
     for (int base = threadIdx.x; base < total; base += 8 * THREADS) {
       float4 v[8];
+      int off[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int e = base + u * THREADS;
-        v[u] = e < total ? *reinterpret_cast<const float4*>(it.A + r0 + 4 * (e % nq) +
-                                                             static_cast<int64_t>(c0 + e / nq) * it.lda)
+        const int c = p2 ? e >> sh : e / nq, q = e - c * nq;
+        off[u] = c * LD + 4 * q;
+        v[u] = e < total ? *reinterpret_cast<const float4*>(it.A + r0 + 4 * q + static_cast<int64_t>(c0 + c) * it.lda)
                          : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = base + u * THREADS;
-        if (e < total) *reinterpret_cast<float4*>(&dst[(e / nq) * LD + 4 * (e % nq)]) = v[u];
-      }
+      for (int u = 0; u < 8; ++u)
+        if (base + u * THREADS < total) *reinterpret_cast<float4*>(&dst[off[u]]) = v[u];
     }
     return;
   }
@@ -138,9 +142,11 @@ __device__ __forceinline__ void store_projection(Smem<CR>& s, int k1, int w, con
 template <int CR>
 __device__ __forceinline__ void chunk_subtract(Smem<CR>& s, int rq, int k1) {
   const int LD = CR + 4;
-  const int ntile = (rq / 4) * (PW / 2);
+  const int nr4 = rq / 4, ntile = nr4 * (PW / 2);
+  const bool p2 = (nr4 & (nr4 - 1)) == 0;
+  const int sh = __ffs(nr4) - 1;
   for (int e = threadIdx.x; e < ntile; e += THREADS) {
-    const int rt = e % (rq / 4), ct = e / (rq / 4);
+    const int ct = p2 ? e >> sh : e / nr4, rt = e - ct * nr4;
     const int r = 4 * rt, jj = 2 * ct;
     float4 x0 = *reinterpret_cast<const float4*>(&s.a[jj * LD + r]);
     float4 x1 = *reinterpret_cast<const float4*>(&s.a[(jj + 1) * LD + r]);
@@ -225,9 +231,11 @@ __device__ __forceinline__ void invert_factor(Smem<CR>& s, int w) {
 template <int CR>
 __device__ __forceinline__ void chunk_solve(const Smem<CR>& s, const float* in, float* out, int rq, int w) {
   const int LD = CR + 4;
-  const int ntile = (rq / 4) * (PW / 2);
+  const int nr4 = rq / 4, ntile = nr4 * (PW / 2);
+  const bool p2 = (nr4 & (nr4 - 1)) == 0;
+  const int sh = __ffs(nr4) - 1;
   for (int e = threadIdx.x; e < ntile; e += THREADS) {
-    const int rt = e % (rq / 4), ct = e / (rq / 4);
+    const int ct = p2 ? e >> sh : e / nr4, rt = e - ct * nr4;
     const int r = 4 * rt, ja = ct, jb = PW - 1 - ct;
     float4 xa = make_float4(0.f, 0.f, 0.f, 0.f), xb = xa;
     const int ea = min(ja + 1, w), eb = min(jb + 1, w);
@@ -253,10 +261,10 @@ __device__ __forceinline__ void chunk_solve(const Smem<CR>& s, const float* in, 
 template <int CR>
 __device__ __forceinline__ void chunk_store(const float* a, const Item& it, int r0, int rows, int c0, int w) {
   const int LD = CR + 4;
-  for (int e = threadIdx.x; e < rows * w; e += THREADS) {
-    const int r = e % rows, jj = e / rows;
-    it.A[r0 + r + static_cast<int64_t>(c0 + jj) * it.lda] = a[jj * LD + r];
-  }
+  // a column per warp, lanes along its rows (no integer division per element)
+  for (int jj = threadIdx.x / 32; jj < w; jj += THREADS / 32)
+    for (int r = threadIdx.x % 32; r < rows; r += 32)
+      it.A[r0 + r + static_cast<int64_t>(c0 + jj) * it.lda] = a[jj * LD + r];
 }
 
 // In-place lower Cholesky of s.g (w x w) by warp 0; returns false on a pivot <= 0.

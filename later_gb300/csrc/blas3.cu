@@ -599,7 +599,8 @@ __global__ void __launch_bounds__(256, 1) potrf_leaf(int nb, float* A, int64_t l
     } else {
       const int ct = tid - 32, nct = static_cast<int>(blockDim.x) - 32;
       // warp 7: the previous diagonal block's inverse into the table, for the triangular solves
-      if (tid >= kPotrfPubCount && k0 > 0 && dinv) potrf_keep_inverse(Ac, k0 - 32, 32, dinv + (k0 / 32 - 1) * kDinvSlot);
+      if (tid >= kPotrfPubCount && k0 > 0 && dinv)
+        potrf_keep_inverse(Ac, k0 - 32, 32, dinv + (k0 / 32 - 1) * kDinvSlot);
       // the previous block's update of the columns right of this block (deferred to this phase; it
       // touches neither this block's columns, which the solve below works on, nor the copy in G)
       if (k0 > 0 && t0 < nb) potrf_syrk(Ac, nb, k0 - 32, 32, t0, nb, ct, nct);
@@ -857,8 +858,8 @@ later_status_t trsm_lln(B3& b, int m, int n, const float* L, int64_t ldl, float*
     const size_t smem = NB * 129 * sizeof(float);
     if (!smem_attr(reinterpret_cast<const void*>(trsm_lln_leaf), smem)) return LATER_ERR_CUDA;
     TraceScope tr(b.st, TRACE_OTHER);
-    LATER_CHECK_CUDA(launch_pdl(trsm_lln_leaf, dim3((n + 7) / 8), dim3(256), smem, b.st, m, n, L, ldl, B, ldb, xh, xl, ldh,
-                                mode_of(b.o.prec)));
+    LATER_CHECK_CUDA(launch_pdl(trsm_lln_leaf, dim3((n + 7) / 8), dim3(256), smem, b.st, m, n, L, ldl, B, ldb, xh, xl,
+                                ldh, mode_of(b.o.prec)));
     note_launch();
     return cuda_status(cudaGetLastError());
   }

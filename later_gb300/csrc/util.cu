@@ -220,7 +220,8 @@ later_status_t convert16(cudaStream_t st, int m, int n, const float* A, int64_t 
     return LATER_OK;
   }
   TraceScope trace(st, TRACE_OTHER);
-  LATER_CHECK_CUDA(launch_pdl(convert_kernel, grid, block, 0, st, m, n, A, lda, hi, lo, ldh, prec, device_status_ptr()));
+  LATER_CHECK_CUDA(
+      launch_pdl(convert_kernel, grid, block, 0, st, m, n, A, lda, hi, lo, ldh, prec, device_status_ptr()));
   note_launch();
   return cuda_status(cudaGetLastError());
 }
