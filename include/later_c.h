@@ -421,9 +421,9 @@ later_status_t later_c_gemm16(later_stream_t stream, char transa, char transb, i
  * LATER_NOALLOC_SCRATCH_FLOATS floats (16 MiB) inside this library, held by
  * every GPU that loads it until exit. The call allocates nothing. The first
  * call on a device looks up the array's address; make it before any stream
- * capture. Requests whose output, rounded up to 128 x 256 tiles, exceeds the
- * array return LATER_ERR_WORKSPACE (use later_c_gemm16 for those). All calls
- * share the array: calls whose kernels overlap on the GPU race on it.
+ * capture. Any output size is accepted: K is split only as far as the array
+ * holds the partial tiles (not at all when they do not fit). All calls share
+ * the array: calls whose kernels overlap on the GPU race on it.
  */
 #define LATER_NOALLOC_SCRATCH_FLOATS 4194304
 later_status_t later_c_gemm16_noalloc(later_stream_t stream, char transa, char transb, int m, int n, int k,

@@ -24,14 +24,16 @@ def _cache_path() -> Path:
 
 
 def _key(shapes, device_name: str) -> str:
-    # log2 histogram of (m, n): batches with the same mix share a tuning result
+    # log2 histogram of (m, n): batches with the same mix share a tuning result, within a factor-of-4
+    # bucket of the batch count (the variants change CTAs per SM, so the count against the SMs matters)
     hist = {}
     for m, n in shapes:
         k = f"{int(math.log2(max(m, 1)))}x{int(math.log2(max(n, 1)))}"
         hist[k] = hist.get(k, 0) + 1
     tot = sum(hist.values())
     sig = ",".join(f"{k}:{round(v / tot, 2)}" for k, v in sorted(hist.items()))
-    return f"{device_name}|{sig}"
+    count = int(math.log2(max(tot, 1))) // 2
+    return f"{device_name}|n{count}|{sig}"
 
 
 def tune(shapes, sample=256, reps=3, use_cache=True, seed=0):

@@ -13,9 +13,12 @@
 // cudaGetSymbolAddress (with that device current) and caches it; make that
 // first call before any stream capture. The array is shared by every call and
 // keeps the last call's contents. Nothing in it has to start at zero: every
-// partial tile is written in full before the reduction reads it. Calls whose
-// kernels overlap on the GPU (different streams, or different host threads)
-// race on the array and must be serialised by the caller.
+// partial tile is written in full before the reduction reads it. Any output
+// size is accepted: the GEMM splits K only as far as the array holds the
+// partial tiles (not at all when one split's tiles do not fit, which is also
+// where the output alone fills the GPU). Calls whose kernels overlap on the GPU
+// (different streams, or different host threads) race on the array and must
+// be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -63,10 +66,6 @@ extern "C" later_status_t later_c_gemm16_noalloc(later_stream_t stream, char tra
   const bool bn = (transb == 'N' || transb == 'n');
   if (lda < (an ? m : k) || ldb < (bn ? k : n) || ldd < m || (beta != 0.f && (!C || ldc < m)))
     return LATER_ERR_INVALID_ARG;
-  // The output rounded up to whole tiles (128 rows x 256 columns, the widest
-  // tile) must fit the array: that is one split's worth of partial tiles.
-  if (round_up(m, 128) * round_up(n, 256) > static_cast<int64_t>(LATER_NOALLOC_SCRATCH_FLOATS))
-    return LATER_ERR_WORKSPACE;
   float* scratch = nullptr;
   LATER_CHECK(scratch_for_current_device(&scratch));
   GemmCall g;

@@ -15,6 +15,12 @@ def test_scaled_batch_same_key():
     assert autotune._key(a, "GB300") == autotune._key(a * 2, "GB300")
 
 
+def test_batch_count_bucket():
+    # the same mix at 10 and at 10,000 matrices is tuned separately (factor-of-4 count buckets)
+    a = [(1000, 64), (5000, 200)] * 5
+    assert autotune._key(a, "GB300") != autotune._key(a * 1000, "GB300")
+
+
 def test_different_mix_or_device_different_key():
     a = [(1000, 64)] * 10
     b = [(8000, 250)] * 10
