@@ -98,8 +98,9 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
+    def __init__(self, index=0, interval_ms=200):
         self.index = index
+        self.interval_ms = interval_ms
         self.proc = None
         self.path = None
 
@@ -109,7 +110,7 @@ class ClockSampler:
             os.close(fd)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -435,6 +436,72 @@ def run_ours(a, rank, world, local_rank):
     bwd, orth = qr_errors_fp64(A0, A, R)
     t_acc = time.perf_counter() - t_acc
 
+    # ---- end to end through the public API with host buffers: later_c_rgsqrf_host copies pinned host A
+    # in and Q, R (upper triangle) out in column chunks overlapped with the factorisation. Measured before
+    # the same-GPU comparators: their own 3 GiB of pinned buffers leave this process's host mappings cold
+    # (the first passes after them ran 2-9x slower), which the reference arm, a process of its own, does
+    # not see either
+    e2e = None
+    if a.e2e_steps > 0:
+        hA = torch.empty(n, m, pin_memory=True).t()  # column-major like A
+        hA.copy_(A0)
+        hQ = torch.empty(n, m, pin_memory=True).t()
+        hR = torch.empty(n, n, pin_memory=True).t()
+
+        def qr_host():
+            lg.later_rgsqrf_host(hA, hQ, hR, A, R, work, hwork, precision=a.precision, cgs2=a.cgs2, leaf=a.leaf,
+                                 panel=a.panel)
+
+        for _ in range(E2E_WARMUP):  # fresh pinned buffers: the first passes run slower
+            qr_host()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        marks = [torch.cuda.Event(enable_timing=True) for _ in range(a.e2e_steps + 1)]
+        eclk = ClockSampler(dev.index or 0, interval_ms=20)
+        eclk.__enter__()
+        time.sleep(0.2)  # the sampler's first reading
+        e0.record(st)
+        marks[0].record(st)
+        for i in range(a.e2e_steps):
+            qr_host()
+            marks[i + 1].record(st)
+        e1.record(st)
+        torch.cuda.synchronize()
+        eclk.__exit__()
+        e2e_ms = e0.elapsed_time(e1) / a.e2e_steps
+        pass_ms = [round(marks[i].elapsed_time(marks[i + 1]), 3) for i in range(a.e2e_steps)]
+        # bytes copied out: Q, and per column chunk of R the rows on and above the diagonal
+        units = -(-n // a.leaf)
+        chunk = max(1, -(-units // 64)) * a.leaf
+        r_bytes = sum(min(chunk, n - c0) * min(n, c0 + chunk) * 4 for c0 in range(0, n, chunk))
+        e2e = {"value": flops / e2e_ms / 1e9, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
+               "api": "later_c_rgsqrf_host (pinned host A in; Q and R's upper triangle out; copies overlapped)",
+               "h2d_bytes_per_step": m * n * 4, "d2h_bytes_per_step": m * n * 4 + r_bytes, "pass_ms": pass_ms,
+               "clocks": eclk.summary()}
+        # the same copies done serially around the device-buffer call, for comparison
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(a.e2e_steps):
+            flat(A).copy_(flat(hA), non_blocking=True)
+            qr()
+            flat(hQ).copy_(flat(A), non_blocking=True)
+            flat(hR).copy_(flat(R), non_blocking=True)
+        e1.record(st)
+        torch.cuda.synchronize()
+        e2e["serial_copies_ms_per_step"] = e0.elapsed_time(e1) / a.e2e_steps
+        # this host's pinned copy bandwidth (1 GiB each way, contiguous): the floor the copies sit on
+        flat_d, flat_h = flat(A), flat(hQ)
+        bw = {}
+        for name, dst, src in (("h2d", flat_d, flat(hA)), ("d2h", flat_h, flat_d)):
+            torch.cuda.synchronize()
+            e0.record(st)
+            dst.copy_(src, non_blocking=True)
+            e1.record(st)
+            torch.cuda.synchronize()
+            bw[name] = flat_d.numel() * 4 / (e0.elapsed_time(e1) * 1e6)
+        e2e["pinned_copy_gbs"] = bw
+
     # ---- the same matrix in a second precision (the reference's FP16 by default)
     alt = None
     if a.alt_precision not in ("none", a.precision):
@@ -516,60 +583,6 @@ def run_ours(a, rank, world, local_rank):
     lg.trace_begin()
     qr()
     tr = lg.trace_end()
-
-    # ---- end to end through the public API with host buffers: later_c_rgsqrf_host copies pinned host A
-    # in and Q, R (upper triangle) out in column chunks overlapped with the factorisation
-    e2e = None
-    if a.e2e_steps > 0:
-        hA = torch.empty(n, m, pin_memory=True).t()  # column-major like A
-        hA.copy_(A0)
-        hQ = torch.empty(n, m, pin_memory=True).t()
-        hR = torch.empty(n, n, pin_memory=True).t()
-
-        def qr_host():
-            lg.later_rgsqrf_host(hA, hQ, hR, A, R, work, hwork, precision=a.precision, cgs2=a.cgs2, leaf=a.leaf,
-                                 panel=a.panel)
-
-        for _ in range(E2E_WARMUP):  # fresh pinned buffers: the first passes run slower
-            qr_host()
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        for _ in range(a.e2e_steps):
-            qr_host()
-        e1.record(st)
-        torch.cuda.synchronize()
-        e2e_ms = e0.elapsed_time(e1) / a.e2e_steps
-        # bytes copied out: Q, and per column chunk of R the rows on and above the diagonal
-        units = -(-n // a.leaf)
-        chunk = max(1, -(-units // 64)) * a.leaf
-        r_bytes = sum(min(chunk, n - c0) * min(n, c0 + chunk) * 4 for c0 in range(0, n, chunk))
-        e2e = {"value": flops / e2e_ms / 1e9, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
-               "api": "later_c_rgsqrf_host (pinned host A in; Q and R's upper triangle out; copies overlapped)",
-               "h2d_bytes_per_step": m * n * 4, "d2h_bytes_per_step": m * n * 4 + r_bytes}
-        # the same copies done serially around the device-buffer call, for comparison
-        torch.cuda.synchronize()
-        e0.record(st)
-        for _ in range(a.e2e_steps):
-            flat(A).copy_(flat(hA), non_blocking=True)
-            qr()
-            flat(hQ).copy_(flat(A), non_blocking=True)
-            flat(hR).copy_(flat(R), non_blocking=True)
-        e1.record(st)
-        torch.cuda.synchronize()
-        e2e["serial_copies_ms_per_step"] = e0.elapsed_time(e1) / a.e2e_steps
-        # this host's pinned copy bandwidth (1 GiB each way, contiguous): the floor the copies sit on
-        flat_d, flat_h = flat(A), flat(hQ)
-        bw = {}
-        for name, dst, src in (("h2d", flat_d, flat(hA)), ("d2h", flat_h, flat_d)):
-            torch.cuda.synchronize()
-            e0.record(st)
-            dst.copy_(src, non_blocking=True)
-            e1.record(st)
-            torch.cuda.synchronize()
-            bw[name] = flat_d.numel() * 4 / (e0.elapsed_time(e1) * 1e6)
-        e2e["pinned_copy_gbs"] = bw
 
     if same_gpu and e2e and "reference_rgsqrf" in same_gpu:
         same_gpu["e2e_speedup_vs_reference"] = same_gpu["reference_rgsqrf"]["e2e_ms"] / e2e["ms_per_step"]
