@@ -226,22 +226,7 @@ def time_reference_gpu(a, A0, ref, steps, warmup, clocks=False):
         A.copy_(A0)
         ref.rgsqrf(A, R, work, hwork)
     torch.cuda.synchronize()
-    evs = []
-    clk = ClockSampler(dev.index or 0) if clocks else None
-    if clk:
-        clk.__enter__()
-    for _ in range(steps):
-        A.copy_(A0)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        ref.rgsqrf(A, R, work, hwork)
-        e1.record(st)
-        evs.append((e0, e1))
-    torch.cuda.synchronize()
-    if clk:
-        clk.__exit__()
-    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
-    bwd, orth = qr_errors_fp64(A0, A, torch.triu(R))
+    # end to end first, right after the warm-up (as in our arm)
     hA = torch.empty(n, m, pin_memory=True).t()
     hA.copy_(A0)
     hQ = torch.empty(n, m, pin_memory=True).t()
@@ -258,17 +243,34 @@ def time_reference_gpu(a, A0, ref, steps, warmup, clocks=False):
     for _ in range(E2E_WARMUP):
         step()
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
     k = max(1, min(steps, 3))
-    for _ in range(k):
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(k + 1)]
+    marks[0].record(st)
+    for i in range(k):
         step()
-    e1.record(st)
+        marks[i + 1].record(st)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / k
+    e2e_ms = marks[0].elapsed_time(marks[k]) / k
+    e2e_pass_ms = [round(marks[i].elapsed_time(marks[i + 1]), 3) for i in range(k)]
+    evs = []
+    clk = ClockSampler(dev.index or 0) if clocks else None
+    if clk:
+        clk.__enter__()
+    for _ in range(steps):
+        A.copy_(A0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        ref.rgsqrf(A, R, work, hwork)
+        e1.record(st)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    if clk:
+        clk.__exit__()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / steps
+    bwd, orth = qr_errors_fp64(A0, A, torch.triu(R))
     out = {"ms_per_step": ms, "value": qr_flops(m, n) / ms / 1e9, "unit": "TFLOP/s",
            "backward_error": bwd, "orthogonality_over_n": orth / n, "e2e_ms": e2e_ms,
-           "e2e": qr_flops(m, n) / e2e_ms / 1e9}
+           "e2e": qr_flops(m, n) / e2e_ms / 1e9, "e2e_pass_ms": e2e_pass_ms}
     if clk:
         out["clocks"] = clk.summary()
     return out
@@ -343,7 +345,7 @@ def run_reference(a, rank, world):
                              "computed": "FP64 on the GPU"},
                 "cpu_baseline": {"value": r["value"], "unit": "TFLOP/s", "cores": ncores, "kind": "reference",
                                  "device": "GPU", "sample": sample},
-                "e2e": {"value": r["e2e"], "unit": "TFLOP/s", "ms_per_step": r["e2e_ms"],
+                "e2e": {"value": r["e2e"], "unit": "TFLOP/s", "ms_per_step": r["e2e_ms"], "pass_ms": r["e2e_pass_ms"],
                         "h2d_bytes_per_step": a.m * a.n * 4, "d2h_bytes_per_step": a.m * a.n * 4 + a.n * a.n * 4},
                 "clocks": r.get("clocks")}
         print(json.dumps(line), flush=True)
@@ -406,41 +408,11 @@ def run_ours(a, rank, world, local_rank):
     if status != 0:
         raise RuntimeError(f"device status {status} during warm-up")
 
-    # ---- timed region (device events per step; restore copy outside the events)
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    launches0 = lg.launch_count()
-    evs = []
-    with ClockSampler(local_rank) as clk:
-        t_wall = time.perf_counter()
-        for _ in range(a.steps):
-            A.copy_(A0)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            qr()
-            e1.record(st)
-            evs.append((e0, e1))
-        torch.cuda.synchronize()
-        t_wall = time.perf_counter() - t_wall
-    if world > 1:
-        dist.barrier()
-    launches = lg.launch_count() - launches0
-    ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    ms_step = sum(ms) / len(ms)
-    clocks = clk.summary()
-
-    # ---- accuracy of the last step, in FP64 on the GPU (outside the timed region)
-    t_acc = time.perf_counter()
-    bwd, orth = qr_errors_fp64(A0, A, R)
-    t_acc = time.perf_counter() - t_acc
-
     # ---- end to end through the public API with host buffers: later_c_rgsqrf_host copies pinned host A
-    # in and Q, R (upper triangle) out in column chunks overlapped with the factorisation. Measured before
-    # the same-GPU comparators: their own 3 GiB of pinned buffers leave this process's host mappings cold
-    # (the first passes after them ran 2-9x slower), which the reference arm, a process of its own, does
-    # not see either
+    # in and Q, R (upper triangle) out in column chunks overlapped with the factorisation. Measured first,
+    # right after the warm-up, like the reference arm (a process of its own): after the FP64 accuracy
+    # check and the same-GPU comparators one pass in three ran about 13 ms slower on some boxes, while in a
+    # process doing nothing else every pass took 27.1-27.8 ms
     e2e = None
     if a.e2e_steps > 0:
         hA = torch.empty(n, m, pin_memory=True).t()  # column-major like A
@@ -501,6 +473,36 @@ def run_ours(a, rank, world, local_rank):
             torch.cuda.synchronize()
             bw[name] = flat_d.numel() * 4 / (e0.elapsed_time(e1) * 1e6)
         e2e["pinned_copy_gbs"] = bw
+
+    # ---- timed region (device events per step; restore copy outside the events)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = lg.launch_count()
+    evs = []
+    with ClockSampler(local_rank) as clk:
+        t_wall = time.perf_counter()
+        for _ in range(a.steps):
+            A.copy_(A0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            qr()
+            e1.record(st)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    if world > 1:
+        dist.barrier()
+    launches = lg.launch_count() - launches0
+    ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    ms_step = sum(ms) / len(ms)
+    clocks = clk.summary()
+
+    # ---- accuracy of the last step, in FP64 on the GPU (outside the timed region)
+    t_acc = time.perf_counter()
+    bwd, orth = qr_errors_fp64(A0, A, R)
+    t_acc = time.perf_counter() - t_acc
 
     # ---- the same matrix in a second precision (the reference's FP16 by default)
     alt = None
