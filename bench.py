@@ -44,6 +44,12 @@ METRIC = "QR TFLOP/s (LAPACK count 2n^2(m-n/3)) at stated ||A-QR||/||A||"
 # Untimed end-to-end passes before the timed ones, in both arms: on GB300 the first passes over freshly
 # pinned host buffers (2.6 GB per QR) take up to twice the steady time (55, 35, 28, 28 ms measured).
 E2E_WARMUP = 4
+# Timed end-to-end passes, in both arms, and the statistic reported: the median pass. On these boxes a
+# pass now and then takes far longer in either arm (153 ms against 27 ms for ours, 153 and 118 against
+# 80 ms for the reference's, the SM clock steady and the measured copy rate unchanged): the host side of
+# the copies, not the factorisation. Every pass and the mean are in the line as well.
+E2E_PASSES = 5
+E2E_STATISTIC = "median of the timed passes (pass_ms lists them; mean_ms_per_step is their mean)"
 
 
 def qr_flops(m, n):
@@ -68,7 +74,7 @@ def parse():
                         "or the reference's MGS-TSQR panels")
     p.add_argument("--cgs2", action="store_true")
     p.add_argument("--seed", type=int, default=1)
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-ref", action="store_true", help="skip the same-GPU reference / cuSOLVER comparators")
     p.add_argument("--no-extras", action="store_true",
@@ -243,15 +249,16 @@ def time_reference_gpu(a, A0, ref, steps, warmup, clocks=False):
     for _ in range(E2E_WARMUP):
         step()
     torch.cuda.synchronize()
-    k = max(1, min(steps, 3))
+    k = E2E_PASSES
     marks = [torch.cuda.Event(enable_timing=True) for _ in range(k + 1)]
     marks[0].record(st)
     for i in range(k):
         step()
         marks[i + 1].record(st)
     torch.cuda.synchronize()
-    e2e_ms = marks[0].elapsed_time(marks[k]) / k
     e2e_pass_ms = [round(marks[i].elapsed_time(marks[i + 1]), 3) for i in range(k)]
+    e2e_mean_ms = marks[0].elapsed_time(marks[k]) / k
+    e2e_ms = statistics.median(e2e_pass_ms)
     evs = []
     clk = ClockSampler(dev.index or 0) if clocks else None
     if clk:
@@ -270,7 +277,7 @@ def time_reference_gpu(a, A0, ref, steps, warmup, clocks=False):
     bwd, orth = qr_errors_fp64(A0, A, torch.triu(R))
     out = {"ms_per_step": ms, "value": qr_flops(m, n) / ms / 1e9, "unit": "TFLOP/s",
            "backward_error": bwd, "orthogonality_over_n": orth / n, "e2e_ms": e2e_ms,
-           "e2e": qr_flops(m, n) / e2e_ms / 1e9, "e2e_pass_ms": e2e_pass_ms}
+           "e2e": qr_flops(m, n) / e2e_ms / 1e9, "e2e_pass_ms": e2e_pass_ms, "e2e_mean_ms": e2e_mean_ms}
     if clk:
         out["clocks"] = clk.summary()
     return out
@@ -345,7 +352,8 @@ def run_reference(a, rank, world):
                              "computed": "FP64 on the GPU"},
                 "cpu_baseline": {"value": r["value"], "unit": "TFLOP/s", "cores": ncores, "kind": "reference",
                                  "device": "GPU", "sample": sample},
-                "e2e": {"value": r["e2e"], "unit": "TFLOP/s", "ms_per_step": r["e2e_ms"], "pass_ms": r["e2e_pass_ms"],
+                "e2e": {"value": r["e2e"], "unit": "TFLOP/s", "ms_per_step": r["e2e_ms"], "statistic": E2E_STATISTIC,
+                        "mean_ms_per_step": r["e2e_mean_ms"], "pass_ms": r["e2e_pass_ms"],
                         "h2d_bytes_per_step": a.m * a.n * 4, "d2h_bytes_per_step": a.m * a.n * 4 + a.n * a.n * 4},
                 "clocks": r.get("clocks")}
         print(json.dumps(line), flush=True)
@@ -441,13 +449,15 @@ def run_ours(a, rank, world, local_rank):
         e1.record(st)
         torch.cuda.synchronize()
         eclk.__exit__()
-        e2e_ms = e0.elapsed_time(e1) / a.e2e_steps
+        mean_ms = e0.elapsed_time(e1) / a.e2e_steps
         pass_ms = [round(marks[i].elapsed_time(marks[i + 1]), 3) for i in range(a.e2e_steps)]
+        e2e_ms = statistics.median(pass_ms)
         # bytes copied out: Q, and per column chunk of R the rows on and above the diagonal
         units = -(-n // a.leaf)
         chunk = max(1, -(-units // 64)) * a.leaf
         r_bytes = sum(min(chunk, n - c0) * min(n, c0 + chunk) * 4 for c0 in range(0, n, chunk))
         e2e = {"value": flops / e2e_ms / 1e9, "unit": "TFLOP/s", "ms_per_step": e2e_ms,
+               "statistic": E2E_STATISTIC, "mean_ms_per_step": mean_ms,
                "api": "later_c_rgsqrf_host (pinned host A in; Q and R's upper triangle out; copies overlapped)",
                "h2d_bytes_per_step": m * n * 4, "d2h_bytes_per_step": m * n * 4 + r_bytes, "pass_ms": pass_ms,
                "clocks": eclk.summary()}
