@@ -99,7 +99,8 @@ def test_rtrmm(cuda, m, n):
     assert err < max(3 * err_o, 1e-6) and err < BOUND["fp16"], (err, err_o)
 
 
-@pytest.mark.parametrize("n,kappa,prec", [(100, 1e2, "fp16"), (1024, 1e2, "fp16"), (4096, 1e2, "fp16"),
+@pytest.mark.parametrize("n,kappa,prec", [(100, 1e2, "fp16"), (250, 1e3, "fp16"), (256, 1e2, "fp16"),
+                                          (1024, 1e2, "fp16"), (4096, 1e2, "fp16"),
                                           (2000, 1e2, "bf16"), (2048, 1e6, "split3"), (6144, 1e2, "fp16"),
                                           (4096, 1e4, "bf16")])
 def test_rpotrf(cuda, n, kappa, prec):
