@@ -20,6 +20,10 @@
 //     kInvMinRows rows are products with the inverse of the factor's 128-column
 //     diagonal block, inverted once, all blocks of a node in one launch
 //     (trtri_blocks_kernel); smaller solves keep the FP32 substitution leaf;
+//   * the blocks the reference hands to cusolverDnSpotrf (at most 2048
+//     columns) are factored by a blocked right-looking loop: per 128-column
+//     block the Cholesky leaf, one solve launch for all rows below, one SPLIT3
+//     lower-triangle update;
 //   * rtrmm adds L21 B1 into C2 in the GEMM epilogue (beta = 1): no tempC;
 //   * 16-bit operand copies are written by the producing leaf (solved X) or
 //     converted once per operand block right before its GEMM;
@@ -29,6 +33,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "blas3.cuh"
@@ -666,9 +671,113 @@ __global__ void __launch_bounds__(256) trtri_blocks_kernel(const float* __restri
   }
 }
 
+// Inverses of 256-column diagonal blocks from the inverses of their two 128-column halves, one CTA per
+// block: for L = [L11 0; L21 L22] (block i: columns [col[i], col[i] + 256), col[i] a multiple of 128),
+// L^-1 = [I1 0; -I2 L21 I1 I2] with I1 = L11^-1 and I2 = L22^-1 read from the 128-column tables (slots
+// col / 64 and col / 64 + 2). P = L21 I1 and X21 = -I2 P are two 128 x 128 x 128 FP32 products in shared
+// memory; the whole inverse goes out as a hi + lo 16-bit pair (ld 256) to slot col[i] / 128.
+constexpr int kMaxInvPairs = 80;
+struct InvPairs {
+  int n;
+  int col[kMaxInvPairs];
+};
+
+// acc[u][v] += sum_k A[k][i] B[k][j], i = ty + 16 u, j = tx + 16 v: Acm holds A column-major (A[i][k] at
+// k * LDL + i), Brm holds B row-major (B[k][j] at k * LDL + j); 256 threads, 8 x 8 outputs each.
+__device__ __forceinline__ void smem_mm128(const float* Acm, const float* Brm, float (&acc)[8][8]) {
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+#pragma unroll 2
+  for (int k = 0; k < NB; ++k) {
+    float a[8], bv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = Acm[k * LDL + ty + 16 * u];
+#pragma unroll
+    for (int v = 0; v < 8; ++v) bv[v] = Brm[k * LDL + tx + 16 * v];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], bv[v], acc[u][v]);
+  }
+}
+
+__device__ __forceinline__ float unsplit(const __half* hi, const __half* lo, int64_t e) {
+  return __half2float(hi[e]) + __half2float(lo[e]) * (1.f / 2048.f);
+}
+
+__global__ void __launch_bounds__(256, 1) inv256_kernel(const float* __restrict__ L, int64_t ldl, InvPairs pairs,
+                                                        const __half* __restrict__ vh_tab,
+                                                        const __half* __restrict__ vl_tab, __half* wh_tab,
+                                                        __half* wl_tab) {
+  griddep_wait();  // inputs come from the previous kernel in the stream
+  griddep_launch();
+  extern __shared__ __align__(16) float sm[];
+  float* S0 = sm;                // L21 (column-major), then I2 (column-major)
+  float* S1 = sm + LDL * NB;     // I1 (row-major)
+  float* S2 = S1 + LDL * NB;     // P = L21 I1 (row-major)
+  const int c = pairs.col[blockIdx.x];
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const __half* i1h = vh_tab + static_cast<int64_t>(c / 64) * (128 * 128);
+  const __half* i1l = vl_tab + static_cast<int64_t>(c / 64) * (128 * 128);
+  const __half* i2h = i1h + 2 * (128 * 128);  // slot c / 64 + 2: the block at column c + 128
+  const __half* i2l = i1l + 2 * (128 * 128);
+  __half* wh = wh_tab + static_cast<int64_t>(c / 128) * (256 * 256);
+  __half* wl = wl_tab + static_cast<int64_t>(c / 128) * (256 * 256);
+  stage_cols(NB, L + (c + NB) + static_cast<int64_t>(c) * ldl, ldl, S0, LDL);
+  // I1 row-major: entry (k, j) of the table (column-major, ld 128) at k * LDL + j
+  for (int e = tid; e < NB * NB; e += 256) {
+    const int k = e & (NB - 1), j = e >> 7;
+    S1[k * LDL + j] = unsplit(i1h, i1l, e);
+  }
+  // the diagonal blocks and the zero upper-right block of the 256 x 256 inverse, straight from the tables
+  for (int e = tid; e < NB * NB; e += 256) {
+    const int i = e & (NB - 1), j = e >> 7;
+    wh[i + j * 256] = i1h[e];
+    wl[i + j * 256] = i1l[e];
+    wh[(NB + i) + (NB + j) * 256] = i2h[e];
+    wl[(NB + i) + (NB + j) * 256] = i2l[e];
+    wh[i + (NB + j) * 256] = __float2half_rn(0.f);
+    wl[i + (NB + j) * 256] = __float2half_rn(0.f);
+  }
+  __syncthreads();
+  float acc[8][8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+  smem_mm128(S0, S1, acc);  // P = L21 I1
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) S2[(ty + 16 * u) * LDL + tx + 16 * v] = acc[u][v];
+  __syncthreads();
+  // I2 column-major into S0 (L21 is no longer needed)
+  for (int e = tid; e < NB * NB; e += 256) {
+    const int i = e & (NB - 1), k = e >> 7;
+    S0[k * LDL + i] = unsplit(i2h, i2l, e);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+  smem_mm128(S0, S2, acc);  // I2 P
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      const int i = ty + 16 * u, j = tx + 16 * v;
+      const float x = -acc[u][v];
+      const __half h = __float2half_rn(x);
+      wh[(NB + i) + j * 256] = h;
+      wl[(NB + i) + j * 256] = __float2half_rn((x - __half2float(h)) * 2048.f);
+    }
+}
+
 constexpr size_t kPotrfLeafSmem = (LDL * NB) * sizeof(float) + (sizeof(PotrfSmem) + 15) / 16 * 16;
 constexpr size_t kTrtriSmem = (2 * LDL * NB + 3 * 1152) * sizeof(float);
 static_assert(kTrtriSmem <= 227 * 1024, "block inverse shared memory");
+constexpr size_t kInv256Smem = 3 * LDL * NB * sizeof(float);
+static_assert(kInv256Smem <= 227 * 1024, "256-column inverse shared memory");
 
 inline int mode_of(int prec) { return prec == LATER_PREC_BF16 ? 1 : (prec == LATER_PREC_SPLIT3 ? 2 : 0); }
 
@@ -713,7 +822,33 @@ struct B3 {
   // Cholesky only: the factor's 32 x 32 diagonal-block inverses (FP32), kept by the Cholesky leaves for the
   // triangular-solve leaves (slot = factor column / 32)
   float* dinv = nullptr;
+  // Cholesky only: blocks of at most kFp32Potrf columns are factored by the blocked loop (potrf_blocked)
+  // rather than by the recursion
+  bool blocked = false;
+  // Cholesky only: inverses of 256-column diagonal blocks (hi + lo, ld 256, slot = col / 128); a solve
+  // against such a block whose inverse is present is one product instead of two and an update between
+  __half* inv2_hi = nullptr;
+  __half* inv2_lo = nullptr;
+  std::vector<char>* inv2_done = nullptr;
 };
+
+// LATER_POTRF_BLOCKED=0 factors the blocks below kFp32Potrf columns by the recursion instead (comparison runs)
+bool potrf_blocked_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("LATER_POTRF_BLOCKED");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+// LATER_POTRF_INV256=0 keeps the solves against 128-column inverses only (comparison runs)
+bool inv2_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("LATER_POTRF_INV256");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 
 // Solves with at least this many rows use the diagonal block's inverse (its
 // one-off inversion is then cheaper than the substitution it replaces).
@@ -721,6 +856,8 @@ constexpr int kInvMinRows = 2048;
 
 constexpr int64_t kInvSlot = 128 * 128;  // 16-bit elements per inverse block (ld 128)
 inline int64_t inv_slots(int n) { return (n + 63) / 64; }
+constexpr int64_t kInv2Slot = 256 * 256;  // 16-bit elements per 256-column inverse (ld 256)
+inline int64_t inv2_slots(int n) { return (n + 127) / 128; }
 inline int64_t dinv_slots(int n) { return (n + 31) / 32; }
 
 // Takes `elems` 16-bit elements from the hwork scratch (256-byte aligned).
@@ -777,6 +914,35 @@ later_status_t gemm(B3& b, char ta, char tb, int M, int N, int K, float alpha, c
 // Updates are FP32 while n <= fp32_lim, tensor-core above.
 later_status_t trsm_rlt(B3& b, int m, int n, const float* L, int64_t ldl, float* B, int64_t ldb, char* xh, char* xl,
                         int64_t ldh, int fp32_lim = kFp32Trsm, int64_t col = -1) {
+  if (n == 2 * NB && b.leaf_gemm && b.inv2_hi && col >= 0 && col % NB == 0 && m >= kInvMinRows && b.inv2_done &&
+      (*b.inv2_done)[col / NB]) {
+    // X = B L^-T against the 256-column block's inverse: one SPLIT3 product replaces the two half-block
+    // products and the update between them
+    B3 sub = b;
+    sub.o.prec = LATER_PREC_SPLIT3;
+    Op16 bb;
+    size_t used = 0;
+    LATER_CHECK(copy16(sub, m, n, B, ldb, &bb, &used));
+    sub.h += used;
+    sub.hcap -= used;
+    const Op16 winv{b.inv2_hi + (col / NB) * kInv2Slot, b.inv2_lo + (col / NB) * kInv2Slot, 2 * NB};
+    GemmCall g;
+    g.ta = 'N';
+    g.tb = 'T';
+    g.M = m;
+    g.N = n;
+    g.K = n;
+    g.A = bb;
+    g.B = winv;
+    g.out.D = B;
+    g.out.ldd = ldb;
+    g.out.Dh = xh;
+    g.out.Dl = xl;
+    g.out.ldh = ldh;
+    g.prec = LATER_PREC_SPLIT3;
+    g.out_prec = xl ? LATER_PREC_SPLIT3 : b.o.prec;
+    return tc_gemm(g, sub.sc, b.st, b.o.budget);
+  }
   if (n <= NB && b.leaf_gemm && b.inv_hi && col >= 0 && m >= kInvMinRows && b.inv_done &&
       (*b.inv_done)[col / 64]) {
     // X = B L^-T as one SPLIT3 tensor-core product with the block's inverse (FP32-level operands)
@@ -960,16 +1126,67 @@ void leaf_blocks(int n, int c, InvBlocks* out, std::vector<char>& done) {
   leaf_blocks(n - n1, c + n1, out, done);
 }
 
-later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
-  if (n <= NB) {
-    const size_t smem = kPotrfLeafSmem;
-    if (!smem_attr(reinterpret_cast<const void*>(potrf_leaf), smem)) return LATER_ERR_CUDA;
-    TraceScope tr(b.st, TRACE_PANEL);
-    float* dinv = b.dinv ? b.dinv + (col / 32) * kDinvSlot : nullptr;
-    LATER_CHECK_CUDA(launch_pdl(potrf_leaf, dim3(1), dim3(256), smem, b.st, n, A, lda, device_status_ptr(), dinv));
-    note_launch();
-    return cuda_status(cudaGetLastError());
+// One Cholesky leaf (n <= NB) at factor column `col`; its 32 x 32 diagonal-block inverses go to the table.
+// The 256-column nodes of the same recursion over n columns from column c (where the solves split
+// 256 columns into two 128-column leaves) whose halves' inverses are in the table; those whose slot
+// is not marked in `done2` are appended to `out` and marked.
+void pair_blocks(int n, int c, const std::vector<char>& done, InvPairs* out, std::vector<char>& done2) {
+  if (n == 2 * NB) {
+    if (c % NB == 0 && done[c / 64] && done[c / 64 + 2] && !done2[c / NB] && out->n < kMaxInvPairs) {
+      out->col[out->n++] = c;
+      done2[c / NB] = 1;
+    }
+    return;
   }
+  if (n < 2 * NB) return;
+  const int n1 = half64(n);
+  pair_blocks(n1, c, done, out, done2);
+  pair_blocks(n - n1, c + n1, done, out, done2);
+}
+
+later_status_t potrf_leaf_launch(B3& b, int n, float* A, int64_t lda, int64_t col) {
+  const size_t smem = kPotrfLeafSmem;
+  if (!smem_attr(reinterpret_cast<const void*>(potrf_leaf), smem)) return LATER_ERR_CUDA;
+  TraceScope tr(b.st, TRACE_PANEL);
+  float* dinv = b.dinv ? b.dinv + (col / 32) * kDinvSlot : nullptr;
+  LATER_CHECK_CUDA(launch_pdl(potrf_leaf, dim3(1), dim3(256), smem, b.st, n, A, lda, device_status_ptr(), dinv));
+  note_launch();
+  return cuda_status(cudaGetLastError());
+}
+
+// Blocked right-looking Cholesky of a block of n <= kFp32Potrf columns (the size the reference hands to
+// cuSOLVER's FP32 Spotrf, Cholesky/later_rpotrf.cu:26-35). Per NB-column block k: the leaf factors the
+// diagonal block; one solve launch gives X = A[k+1:, k] L_kk^{-T} for all rows below, in place, with its
+// hi + lo FP16 pair; one lower-triangle SPLIT3 tensor-core product applies A[k+1:, k+1:] -= X X^T. Three
+// launches per block column instead of the recursion's chain of ever smaller solves, updates and
+// conversions; every update is FP32-level, as in the recursion.
+later_status_t potrf_blocked(B3& b, int n, float* A, int64_t lda, int64_t col) {
+  for (int k0 = 0; k0 < n; k0 += NB) {
+    const int w = std::min(NB, n - k0);
+    float* Akk = A + k0 + static_cast<int64_t>(k0) * lda;
+    LATER_CHECK(potrf_leaf_launch(b, w, Akk, lda, col + k0));
+    const int r = n - k0 - w;
+    if (r == 0) break;
+    const int64_t ldx = round_up(r, 8);
+    B3 s3 = b;
+    s3.o.prec = LATER_PREC_SPLIT3;
+    size_t used = 0;
+    char* xh = take16(s3, ldx * w, &used);
+    if (!xh) return LATER_ERR_WORKSPACE;
+    char* xl = xh + ldx * w * 2;
+    s3.h += used;
+    s3.hcap -= used;
+    LATER_CHECK(trsm_rlt(s3, r, w, Akk, lda, Akk + w, lda, xh, xl, ldx, w, col + k0));
+    const Op16 x{xh, xl, ldx};
+    LATER_CHECK(gemm(s3, 'N', 'T', r, r, w, -1.f, x, x, 1.f, Akk + w + static_cast<int64_t>(w) * lda, lda, nullptr,
+                     nullptr, 0, 1));
+  }
+  return LATER_OK;
+}
+
+later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
+  if (n <= NB) return potrf_leaf_launch(b, n, A, lda, col);
+  if (n <= kFp32Potrf && b.tc_small && b.blocked) return potrf_blocked(b, n, A, lda, col);
   const int n1 = half64(n), n2 = n - n1;
   LATER_CHECK(potrf_rec(b, n1, A, lda, col));
   if (b.leaf_gemm && b.inv_hi && b.inv_done && n2 >= kInvMinRows) {
@@ -983,6 +1200,20 @@ later_status_t potrf_rec(B3& b, int n, float* A, int64_t lda, int64_t col = 0) {
                                   static_cast<const float*>(A - col - col * lda), lda, blk, b.inv_hi, b.inv_lo));
       note_launch();
       LATER_CHECK_CUDA(cudaGetLastError());
+    }
+    if (b.inv2_hi && b.inv2_done) {
+      // the solve's 256-column nodes: their inverses from the two halves' (one launch)
+      InvPairs prs{};
+      pair_blocks(n1, static_cast<int>(col), *b.inv_done, &prs, *b.inv2_done);
+      if (prs.n > 0) {
+        if (!smem_attr(reinterpret_cast<const void*>(inv256_kernel), kInv256Smem)) return LATER_ERR_CUDA;
+        LATER_CHECK_CUDA(launch_pdl(inv256_kernel, dim3(prs.n), dim3(256), kInv256Smem, b.st,
+                                    static_cast<const float*>(A - col - col * lda), lda, prs,
+                                    static_cast<const __half*>(b.inv_hi), static_cast<const __half*>(b.inv_lo),
+                                    b.inv2_hi, b.inv2_lo));
+        note_launch();
+        LATER_CHECK_CUDA(cudaGetLastError());
+      }
     }
   }
   const bool fp32 = n <= kFp32Potrf;
@@ -1061,7 +1292,8 @@ int64_t rpotrf_hwork(int n, const Options& o) {
   const int64_t h = n / 2 + 64;
   const int64_t inv = 2 * inv_slots(n) * kInvSlot + 256;
   const int64_t dinv = dinv_slots(n) * kDinvSlot * 2 + 256;  // FP32 entries, in 16-bit units
-  return inv + dinv +
+  const int64_t inv2 = n > kFp32Potrf ? 2 * inv2_slots(n) * kInv2Slot + 256 : 0;
+  return inv + dinv + inv2 +
          (round_up(h, 8) * h + 2 * round_up(h / 2 + 64, 8) * (h / 2 + 64) + round_up(h, 8) * NB + 4096) * 2;
 }
 int64_t splitk_work() { return static_cast<int64_t>(num_sms()) * 128 * 256 * 2 + 256; }
@@ -1146,6 +1378,7 @@ later_status_t rpotrf(cudaStream_t st, char uplo, int n, float* A, int64_t lda, 
   if (n > NB) {
     // inverses of the factor's diagonal blocks first in hwork; the recursion's scratch after them
     b.tc_small = true;
+    b.blocked = potrf_blocked_enabled();
     b.leaf_gemm = o.prec != LATER_PREC_SPLIT3;  // SPLIT3 keeps FP32 substitution in the block solves
     const int64_t slots = inv_slots(n) * kInvSlot;
     if (b.leaf_gemm) {
@@ -1157,11 +1390,20 @@ later_status_t rpotrf(cudaStream_t st, char uplo, int n, float* A, int64_t lda, 
     const uintptr_t d = (reinterpret_cast<uintptr_t>(b.h) + skip + 255) & ~uintptr_t(255);
     b.dinv = reinterpret_cast<float*>(d);
     skip = (d - reinterpret_cast<uintptr_t>(b.h)) + static_cast<size_t>(dinv_slots(n)) * kDinvSlot * sizeof(float);
+    if (b.leaf_gemm && n > kFp32Potrf && inv2_enabled()) {
+      // then the 256-column inverses (256-byte aligned)
+      const uintptr_t w = (reinterpret_cast<uintptr_t>(b.h) + skip + 255) & ~uintptr_t(255);
+      b.inv2_hi = reinterpret_cast<__half*>(w);
+      b.inv2_lo = b.inv2_hi + inv2_slots(n) * kInv2Slot;
+      skip = (w - reinterpret_cast<uintptr_t>(b.h)) + static_cast<size_t>(2 * inv2_slots(n) * kInv2Slot) * 2;
+    }
     b.h += skip;
     b.hcap = b.hcap > skip ? b.hcap - skip : 0;
   }
   std::vector<char> done(static_cast<size_t>(inv_slots(std::max(n, 1))), 0);
+  std::vector<char> done2(static_cast<size_t>(inv2_slots(std::max(n, 1))), 0);
   b.inv_done = &done;
+  b.inv2_done = &done2;
   return potrf_rec(b, n, A, lda);
 }
 
