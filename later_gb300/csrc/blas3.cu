@@ -19,7 +19,10 @@
 //     (hi + lo operands, FP32-level), and the triangular solves with at least
 //     kInvMinRows rows are products with the inverse of the factor's 128-column
 //     diagonal block, inverted once, all blocks of a node in one launch
-//     (trtri_blocks_kernel); smaller solves keep the FP32 substitution leaf;
+//     (trtri_blocks_kernel); where such a solve splits 256 columns into two
+//     128-column blocks, it is one product with the 256-column block's inverse
+//     (inv256_kernel, built from the two halves' inverses); smaller solves keep
+//     the FP32 substitution leaf;
 //   * the blocks the reference hands to cusolverDnSpotrf (at most 2048
 //     columns) are factored by a blocked right-looking loop: per 128-column
 //     block the Cholesky leaf, one solve launch for all rows below, one SPLIT3

@@ -1,13 +1,15 @@
-"""rpotrf's alternative schedules agree (the blocked loop below 2048 columns, the 256-column inverse solves).
+"""rpotrf's alternative schedules give the same factor to the arithmetic's accuracy.
 
-By default such a block (the size the reference hands to cuSOLVER's FP32 Spotrf,
-Cholesky/later_rpotrf.cu:26-35) is factored by the blocked right-looking loop: per
-128-column block the Cholesky leaf, one solve launch for every row below and one
-SPLIT3 lower-triangle update. A process started with LATER_POTRF_BLOCKED=0 factors
-it by the split-in-half recursion instead. Both are FP32-level: on the same input
-the blocked factor's FP64 backward error is at most twice the recursion's (it is
-usually smaller: fewer roundings of each update), both are within the FP32-level
-bound of the SPLIT3 tests, and the two factors agree far below FP16 rounding.
+A block of at most 2048 columns (the size the reference hands to cuSOLVER's FP32
+Spotrf, Cholesky/later_rpotrf.cu:26-35) is by default factored by the blocked
+right-looking loop: per 128-column block the Cholesky leaf, one solve launch for
+every row below and one SPLIT3 lower-triangle update. A process started with
+LATER_POTRF_BLOCKED=0 factors it by the split-in-half recursion instead. Both are
+FP32-level: on the same input the blocked factor's FP64 backward error is at most
+twice the recursion's (it is usually smaller: fewer roundings of each update), both
+are within the FP32-level bound of the SPLIT3 tests, and the two factors agree far
+below FP16 rounding. The 256-column inverse solves above 2048 columns have their own
+switch and test below.
 """
 import os
 import subprocess
