@@ -575,6 +575,51 @@ __device__ __forceinline__ void potrf_syrk(float* Ac, int nb, int k0, int kb, in
   }
 }
 
+// A[i][j] -= sum_{l < kw} A[i][kc + l] A[j][kc + l] for the lower entries of the w x w diagonal block at
+// (j0, j0), w <= 32, j0 a multiple of 4: lane i of warp g computes row i, columns 4 g .. 4 g + 3
+// (256 threads; no barrier inside).
+__device__ __forceinline__ void potrf_diag_update(float* Ac, int kc, int kw, int j0, int w) {
+  const int i = threadIdx.x & 31, g = threadIdx.x >> 5;
+  if (4 * g >= w) return;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+  for (int l = 0; l < kw; ++l) {
+    const float a = i < w ? Ac[(kc + l) * LDL + j0 + i] : 0.f;
+    const float4 b = *reinterpret_cast<const float4*>(&Ac[(kc + l) * LDL + j0 + 4 * g]);
+    acc[0] = fmaf(a, b.x, acc[0]);
+    acc[1] = fmaf(a, b.y, acc[1]);
+    acc[2] = fmaf(a, b.z, acc[2]);
+    acc[3] = fmaf(a, b.w, acc[3]);
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const int j = 4 * g + v;
+    if (i < w && j < w && j <= i) Ac[(j0 + j) * LDL + j0 + i] -= acc[v];
+  }
+}
+
+// Row r: A[r][j0 + j] -= sum_{l < kw} A[r][kc + l] A[j0 + j][kc + l] for j < w (w <= 32, j0 a multiple of 4).
+__device__ __forceinline__ void potrf_row_update(float* Ac, int r, int kc, int kw, int j0, int w) {
+  float acc[32];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) acc[j] = 0.f;
+#pragma unroll 2
+  for (int l = 0; l < kw; ++l) {
+    const float a = Ac[(kc + l) * LDL + r];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float4 b = *reinterpret_cast<const float4*>(&Ac[(kc + l) * LDL + j0 + 4 * q]);
+      acc[4 * q] = fmaf(a, b.x, acc[4 * q]);
+      acc[4 * q + 1] = fmaf(a, b.y, acc[4 * q + 1]);
+      acc[4 * q + 2] = fmaf(a, b.z, acc[4 * q + 2]);
+      acc[4 * q + 3] = fmaf(a, b.w, acc[4 * q + 3]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 32; ++j)
+    if (j < w) Ac[(j0 + j) * LDL + r] -= acc[j];
+}
+
 // The w x w diagonal block at (cb, cb) of Ac, inverted by one warp into the table slot `out`.
 __device__ __forceinline__ void potrf_keep_inverse(const float* Ac, int cb, int w, float* out) {
   const int lane = threadIdx.x & 31;
@@ -612,9 +657,13 @@ __global__ void __launch_bounds__(256, 1) potrf_leaf(int nb, float* A, int64_t l
       // the previous block's update of the columns right of this block (deferred to this phase; it
       // touches neither this block's columns, which the solve below works on, nor the copy in G)
       if (k0 > 0 && t0 < nb) potrf_syrk(Ac, nb, k0 - 32, 32, t0, nb, ct, nct);
-      // rows below the block: x R = a with R = L_D^T, eight columns per published pivot group (warps 1..6)
+      // rows below the block: x R = a with R = L_D^T, eight columns per published pivot group (warps 1..6);
+      // first each row's share of the previous block's update of this block's columns (the end of the
+      // previous phase updated only the diagonal block)
       if (tid < kPotrfPubCount) {
         const int nsv = kPotrfPubCount - 32;
+        if (k0 > 0)
+          for (int r = t0 + ct; r < nb; r += nsv) potrf_row_update(Ac, r, k0 - 32, 32, k0, kb);
         for (int b = 0; b < kb; b += 8) {
           asm volatile("bar.sync %0, %1;" ::"r"(kPotrfPub + b / 8), "r"(kPotrfPubCount) : "memory");
           for (int r = t0 + ct; r < nb; r += nsv) rows_solve_group(Ac + k0 * LDL, LDL, kb, r, ps.Rc, ps.rinv, b);
@@ -628,8 +677,10 @@ __global__ void __launch_bounds__(256, 1) potrf_leaf(int nb, float* A, int64_t l
       const int i = e & 31, j = e >> 5;
       if (j <= i && i < kb) Ac[(k0 + j) * LDL + k0 + i] = ps.Rc[i * RCS + j];
     }
-    // this block's update of the next block's columns only; the rest waits for the next phase
-    if (t0 < nb) potrf_syrk(Ac, nb, k0, kb, t0, min(nb, t0 + 32), tid, blockDim.x);
+    // this block's update of the next diagonal block only; the rows below it follow in the next phase
+    // (each by the thread that solves it), the columns further right in the phase after
+    // (it reads only rows below this diagonal block, which the write-back above does not touch)
+    if (t0 < nb) potrf_diag_update(Ac, k0, kb, t0, min(32, nb - t0));
     __syncthreads();
   }
   if (bad && tid == 0) report(status, DEV_NUMERIC);
