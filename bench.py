@@ -9,6 +9,12 @@ plain FP16 updates (the reference's only mode) and reported under
 `alt_precision`. The metric is the reference's QR rate, 2 n^2 (m - n/3) / t
 (test/test_qr.cu:85-86), in TFLOP/s, reported beside the backward error.
 
+The same line carries, under `configs`, the QR precision sweep (rgsqrf and rhouqr
+over SVD-built 16384 x 16384 and 65536 x 4096 inputs, kappa 1e1 / 1e3 / 1e5, every
+precision mode, with probe-estimated FP64 errors), the Cholesky + refined SPD solve,
+the batched QR and the least-squares serving loop; `--config sweep | spd | batched |
+serve` runs one of them alone.
+
 A step is one QR of the full matrix. The matrix (1 GiB) is larger than L2, and
 it is restored from a pristine device copy before each step (outside the
 per-step events). `value` is the device-timed rate with inputs resident in
@@ -28,6 +34,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -79,12 +86,15 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     p.add_argument("--no-ref", action="store_true", help="skip the same-GPU reference / cuSOLVER comparators")
     p.add_argument("--no-extras", action="store_true",
-                   help="qr: skip the C3 / C4 / C5 configurations that follow the headline in the same line")
+                   help="qr: skip the C2 sweep and the C3 / C4 / C5 configurations that follow the headline in "
+                        "the same line")
     p.add_argument("--cpu-m", type=int, default=16384, help="CPU sample rows")
     p.add_argument("--cpu-n", type=int, default=1024, help="CPU sample columns")
-    p.add_argument("--config", default="qr", choices=["qr", "spd", "batched", "serve"],
+    p.add_argument("--config", default="qr", choices=["qr", "spd", "batched", "serve", "sweep"],
                    help="qr: rgsqrf (default, the headline); spd: rpotrf + FP64-refined SPD solve; "
-                        "batched: 4096 uneven tall-skinny QRs in one persistent launch; serve: LS serving loop")
+                        "batched: 4096 uneven tall-skinny QRs in one persistent launch; serve: LS serving loop; "
+                        "sweep: rgsqrf / rhouqr precision sweep over SVD-built inputs")
+    p.add_argument("--sweep-small", action="store_true", help="sweep: smaller shapes (a quick check)")
     p.add_argument("--kappa", type=float, default=1e2, help="spd: condition number")
     p.add_argument("--count", type=int, default=4096, help="batched: number of matrices")
     p.add_argument("--rates", type=float, nargs="*", default=None,
@@ -687,7 +697,8 @@ def run_ours(a, rank, world, local_rank):
         ref = None if a.no_ref else reference_gpu_harness()
         extras = {}
         t_x = time.perf_counter()
-        for name, fn in (("C3_spd_kappa1e2", lambda: spd_result(a, 16384, 1e2, "fp16", 3, 1, cpu=not a.no_cpu, ref=ref)),
+        for name, fn in (("C2_sweep", lambda: sweep_summary(a)),
+                         ("C3_spd_kappa1e2", lambda: spd_result(a, 16384, 1e2, "fp16", 3, 1, cpu=not a.no_cpu, ref=ref)),
                          ("C3_spd_kappa1e6", lambda: spd_result(a, 16384, 1e6, "fp16", 3, 1, cpu=False, ref=None)),
                          ("C4_batched", lambda: batched_result(a, 4096, 3, 2)),
                          ("C5_serve", lambda: serve_result(a, 1000, [0.5, 2.0, 8.0], 4, 200))):
@@ -978,6 +989,133 @@ def batched_result(a, count, steps, warmup):
                                        "sample": f"{len(sub)} matrices of the same distribution"}}
 
 
+def qr_errors_probe(A0d, AX, X, Q, R):
+    """||A - QR||_F / ||A||_F and ||I - Q^T Q||_F estimated in FP64 from k Gaussian probe vectors X (n x k):
+    E[||E X||_F^2] = k ||E||_F^2 for X with i.i.d. N(0,1) entries (relative spread about sqrt(2 / k)).
+    A0d: A in FP64; AX = A0d X, computed once per input."""
+    import torch
+    k = X.shape[1]
+    Qd = Q.double()
+    E = AX - Qd @ (torch.triu(R).double() @ X)
+    bwd = float(torch.sqrt((E * E).sum() / k) / torch.linalg.norm(A0d))
+    F = Qd.t() @ (Qd @ X) - X
+    orth = float(torch.sqrt((F * F).sum() / k))
+    return bwd, orth
+
+
+def sweep_result(a, probes=64):
+    """The QR precision sweep: A = U diag(sigma) V^T (U, V orthonormal from Gaussian QR with the signs of R's
+    diagonal moved into Q, sigma geometric from 1 to 1/kappa), 16384 x 16384 and 65536 x 4096, kappa in
+    {1e1, 1e3, 1e5}; rgsqrf in FP16, BF16, SPLIT3 and SPLIT2, with and without CGS2 for FP16 and SPLIT2, and
+    rhouqr in FP16, BF16 and SPLIT3. Per run: the median of two timed calls after one untimed one (device
+    time, workspaces preallocated, the input restored before each call outside the events), and the
+    backward error and orthogonality estimated in FP64 from Gaussian probes."""
+    import torch
+    import later_gb300 as lg
+    shapes = [(16384, 16384), (65536, 4096)] if not a.sweep_small else [(4096, 2048), (16384, 1024)]
+    kappas = [1e1, 1e3, 1e5]
+    rg_modes = [("fp16", False), ("bf16", False), ("split3", False), ("split2", False), ("fp16", True),
+                ("split2", True)]
+    rh_modes = ["fp16", "bf16", "split3"]
+    results = []
+
+    def timed(restore, call, warm=1, reps=2):
+        ts = []
+        for it in range(warm + reps):
+            restore()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            call()
+            e1.record()
+            torch.cuda.synchronize()
+            if it >= warm:
+                ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    for m, n in shapes:
+        g = torch.Generator(device="cuda").manual_seed(a.seed + m + n)
+
+        def haar(rows, cols):
+            q, r = torch.linalg.qr(torch.randn(rows, cols, generator=g, device="cuda"))
+            return q * torch.sign(torch.diagonal(r))[None, :]
+
+        U, V = haar(m, n), haar(n, n)
+        X = torch.randn(n, probes, generator=g, device="cuda", dtype=torch.float64)
+        flops = qr_flops(m, n)
+        for kappa in kappas:
+            sig = torch.logspace(0.0, -math.log10(kappa), n, device="cuda")
+            A0 = lg.empty_colmajor(m, n)
+            A0.copy_((U * sig[None, :]) @ V.t())
+            A0d = A0.double()
+            AX = A0d @ X
+            A = lg.empty_colmajor(m, n)
+            for prec, cgs2 in rg_modes:
+                R = lg.empty_colmajor(n, n)
+                lw, lh = lg.rgsqrf_bufsize(m, n, prec, cgs2)
+                work = torch.empty(lw, device="cuda")
+                hwork = torch.empty(lh, dtype=torch.float16, device="cuda")
+                row = {"routine": "rgsqrf", "m": m, "n": n, "kappa": kappa, "precision": prec, "cgs2": cgs2}
+                try:
+                    ms = timed(lambda: A.copy_(A0),
+                               lambda: lg.later_rgsqrf(A, R, work, hwork, precision=prec, cgs2=cgs2))
+                    st = lg.device_status()
+                    bwd, orth = qr_errors_probe(A0d, AX, X, A, R)
+                    row.update({"ms": round(ms, 3), "tflops": round(flops / ms / 1e9, 1), "backward_error": bwd,
+                                "orthogonality_fro": orth, "orthogonality_over_n": orth / n, "status": st})
+                except lg.LaterError as e:
+                    row["error"] = str(e)
+                results.append(row)
+                del R, work, hwork
+            for prec in rh_modes:
+                W, R = lg.empty_colmajor(m, n), lg.empty_colmajor(n, n)
+                lw, lh = lg.rhouqr_bufsize(m, n, prec)
+                work = torch.empty(lw, device="cuda")
+                hwork = torch.empty(lh, dtype=torch.float16, device="cuda")
+                row = {"routine": "rhouqr", "m": m, "n": n, "kappa": kappa, "precision": prec, "cgs2": False}
+                try:
+                    ms = timed(lambda: A.copy_(A0), lambda: lg.later_rhouqr(A, W, R, work, hwork, precision=prec))
+                    st = lg.device_status()
+                    lg.later_ormqr(W, A)  # Q = I - W Y^T over W, for the errors (not timed)
+                    st = st or lg.device_status()
+                    bwd, orth = qr_errors_probe(A0d, AX, X, W, R)
+                    row.update({"ms": round(ms, 3), "tflops": round(flops / ms / 1e9, 1), "backward_error": bwd,
+                                "orthogonality_fro": orth, "orthogonality_over_n": orth / n, "status": st})
+                except lg.LaterError as e:
+                    row["error"] = str(e)
+                results.append(row)
+                del W, R, work, hwork
+            del A0, A0d, AX, A
+            torch.cuda.empty_cache()
+        del U, V
+    return results
+
+
+def sweep_summary(a):
+    res = sweep_result(a)
+    head = [r for r in res if r["routine"] == "rgsqrf" and r["precision"] == "split2" and not r["cgs2"]
+            and "tflops" in r]
+    shapes = list(dict.fromkeys(f"{r['m']}x{r['n']}" for r in res))
+    return {"workload": "A = U diag(sigma) V^T, sigma geometric 1..1/kappa, kappa 1e1, 1e3, 1e5; shapes "
+                        + ", ".join(shapes) + "; rgsqrf fp16 / bf16 / split3 / split2 (+ CGS2 for fp16, split2), "
+                        "rhouqr fp16 / bf16 / split3",
+            "value": min(r["tflops"] for r in head) if head else None, "unit": "TFLOP/s (2n^2(m-n/3))",
+            "value_is": "the lowest rgsqrf SPLIT2 rate over the sweep's shapes and kappas",
+            "errors": "estimated in FP64 from 64 Gaussian probe vectors (relative spread about 18%)",
+            "timing": "device time, median of 2 calls after 1 untimed, through the Python API with "
+                      "preallocated workspaces",
+            "results": res}
+
+
+def run_sweep(a):
+    t0 = time.perf_counter()
+    r = sweep_summary(a)
+    print(json.dumps({"metric": "QR precision sweep: TFLOP/s (2n^2(m-n/3)) with backward error and orthogonality",
+                      "n_gpus": 1, "higher_is_better": True, "data": "synthetic",
+                      "config": {"workload": r.pop("workload")}, **r,
+                      "wall_s": round(time.perf_counter() - t0, 1)}), flush=True)
+
+
 def run_batched(a):
     r = batched_result(a, a.count, a.steps, a.warmup)
     print(json.dumps({"metric": "batched QR TFLOP/s (sum 2n^2(m-n/3)) and matrices/s", "n_gpus": 1,
@@ -1086,7 +1224,7 @@ def main():
         run_gemm_only(a)
         return
     if a.config != "qr" and a.impl == "ours":
-        {"spd": run_spd, "batched": run_batched, "serve": run_serve}[a.config](a)
+        {"spd": run_spd, "batched": run_batched, "serve": run_serve, "sweep": run_sweep}[a.config](a)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
