@@ -471,6 +471,10 @@ struct HCtx {
 
 inline char* at16(char* base, int64_t ld, int64_t r, int64_t c) { return base ? base + (r + c * ld) * 2 : nullptr; }
 
+// Longest tensor-core accumulation chain of rhouqr's SPLIT3 projections (rows of K; a multiple of 8, so
+// that the 16-bit row offsets stay 16-byte aligned for the tensor maps).
+constexpr int kSplit3ChainRows = 1024;
+
 // C (k1 x k2) = X^T Z over mr rows, then Z' = Z - V C, through the tensor
 // cores (16-bit copies xh/zh/vh) or FP32 SIMT.
 later_status_t apply_block(HCtx& c, bool tc, int mr, int k1, int k2, const float* X, int64_t ldx, const char* xh,
@@ -489,22 +493,37 @@ later_status_t apply_block(HCtx& c, bool tc, int mr, int k1, int k2, const float
                                            (reinterpret_cast<uintptr_t>(c.ws->cursor()) + 255) & ~uintptr_t(255))
                                      : nullptr;
   if (sc.partial_floats > 0) sc.partial_floats -= 64;
-  GemmCall tn;
-  tn.ta = 'T';
-  tn.tb = 'N';
-  tn.M = k1;
-  tn.N = k2;
-  tn.K = mr;
-  tn.A = Op16{xh, xl, c.ldh};
-  tn.B = Op16{zh, zl, c.ldh};
-  tn.out.D = c.work32;
-  tn.out.ldd = c.ldwk;
-  tn.out.Dh = c.workh;
-  tn.out.Dl = c.workl;
-  tn.out.ldh = c.ldwk;
-  tn.prec = c.o.prec;
-  tn.out_prec = c.o.prec;
-  LATER_CHECK(tc_gemm(tn, sc, c.st, c.o.budget));
+  // SPLIT3: X^T Z over K = mr rows is summed in chains of at most kSplit3ChainRows rows, each chain's
+  // tensor-core result added to the FP32 product in the epilogue (beta = 1, round to nearest). The
+  // tensor cores' FP32 accumulation over one chain of all mr rows lets rhouqr's backward error grow with m
+  // (R12 is read off the updated A2, so the projection's error enters it directly); bounded chains keep it
+  // at the level of short K.
+  const int chain = c.o.prec == LATER_PREC_SPLIT3 ? kSplit3ChainRows : mr;
+  for (int r = 0; r < mr; r += chain) {
+    const int kk = std::min(chain, mr - r);
+    const bool last = r + kk >= mr;
+    GemmCall tn;
+    tn.ta = 'T';
+    tn.tb = 'N';
+    tn.M = k1;
+    tn.N = k2;
+    tn.K = kk;
+    tn.A = Op16{xh + 2 * static_cast<int64_t>(r), xl ? xl + 2 * static_cast<int64_t>(r) : nullptr, c.ldh};
+    tn.B = Op16{zh + 2 * static_cast<int64_t>(r), zl ? zl + 2 * static_cast<int64_t>(r) : nullptr, c.ldh};
+    if (r > 0) {
+      tn.beta = 1.f;
+      tn.out.C = c.work32;
+      tn.out.ldc = c.ldwk;
+    }
+    tn.out.D = c.work32;
+    tn.out.ldd = c.ldwk;
+    tn.out.Dh = last ? c.workh : nullptr;
+    tn.out.Dl = last ? c.workl : nullptr;
+    tn.out.ldh = c.ldwk;
+    tn.prec = c.o.prec;
+    tn.out_prec = c.o.prec;
+    LATER_CHECK(tc_gemm(tn, sc, c.st, c.o.budget));
+  }
   GemmCall nn;
   nn.ta = 'N';
   nn.tb = 'N';
