@@ -129,3 +129,40 @@ def test_mgs_panels_match_oracle_elementwise(cuda, m, n, prec, tol):
     eq = np.abs(Q - Qo).max() / np.abs(Qo).max()
     er = np.abs(np.triu(Rc) - np.triu(Ro)).max() / np.abs(Ro).max()
     assert eq <= tol and er <= tol, (eq, er)
+
+
+def _gpu_svd(m, n, kappa, seed):
+    """A = U diag(sigma) V^T built on the GPU: U, V from Gaussian QR with the signs of R's diagonal moved
+    into Q, sigma geometric from 1 to 1/kappa (the sweep's construction, at sizes the host would be slow at)."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+
+    def haar(r, c):
+        q, rr = torch.linalg.qr(torch.randn(r, c, generator=g, device="cuda"))
+        return q * torch.sign(torch.diagonal(rr))[None, :]
+
+    U, V = haar(m, n), haar(n, n)
+    sig = torch.logspace(0.0, -float(np.log10(kappa)), n, device="cuda")
+    A = lg.empty_colmajor(m, n)
+    A.copy_((U * sig[None, :]) @ V.t())
+    return A
+
+
+def test_rhouqr_split3_tall_stays_at_split3_level(cuda):
+    """65536 x 1024, kappa 1e3: rhouqr's R12 is read off the updated A2, so the error of its projection
+    W1^T A2 (K = 65536) enters the backward error directly. With the projection's tensor-core accumulation
+    chains bounded, the FP64 backward error stays at rgsqrf's SPLIT3 level on the same input (9.4e-7
+    against 6.4e-7 measured; 9.8e-6 before the chains were bounded)."""
+    m, n = 65536, 1024
+    A0 = _gpu_svd(m, n, 1e3, seed=m + n)
+    A = lg.empty_colmajor(m, n)
+    A.copy_(A0)
+    W, R = lg.later_rhouqr(A, precision="split3")
+    lg.later_ormqr(W, A)
+    assert lg.device_status() == 0
+    b_h, o_h = qr_errors_fp64(A0, W, R)
+    A.copy_(A0)
+    R2 = lg.later_rgsqrf(A, precision="split3")
+    assert lg.device_status() == 0
+    b_g, _ = qr_errors_fp64(A0, A, R2)
+    assert b_h <= 3e-6 and b_h <= 3.0 * b_g, (b_h, b_g)
+    assert o_h / n <= 1e-7, o_h
