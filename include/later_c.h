@@ -353,7 +353,9 @@ later_server_t* later_c_ls_server_create(int device, int slots, int64_t hbm_budg
                                          const later_options_t* opt, int max_iter, double tol);
 /* Queues a request; returns a ticket >= 0, or -later_status_t (a request
  * larger than the whole budget is refused with -LATER_ERR_WORKSPACE). The
- * host buffers must stay valid until later_c_ls_server_wait returns. */
+ * host buffers must stay valid until later_c_ls_server_wait returns. They may
+ * be pageable (the driver stages each copy); pinned buffers (cudaHostAlloc /
+ * cudaHostRegister) let a slot's copies run asynchronously with the device. */
 int64_t later_c_ls_server_submit(later_server_t* s, const later_ls_request_t* req);
 /* Blocks until the request is done and fills `out`. */
 later_status_t later_c_ls_server_wait(later_server_t* s, int64_t ticket, later_ls_result_t* out);
